@@ -1,0 +1,121 @@
+/*
+ * xgrid_gb300.h — C ABI of the GB300 stencil backend.
+ *
+ * Two kinds of shared objects export this ABI:
+ *
+ *  1. libxgrid_gb300.so, the runtime (xgrid_gb300/csrc/xgrid_runtime.cu): error
+ *     channel, device-resident boundary masks and their index tables, and the
+ *     CUDA-graph call cache.
+ *  2. One generated module per @xgrid.kernel (cacheroot/<md5>.cu.so), which
+ *     exports one entry point  xg_kernel_<name>  of type xg_entry_fn.
+ *
+ * Every function returns 0 on success and a negative status on failure; the
+ * message is then available from xg_last_error() (thread-local).  Python raises
+ * it as an Exception, which keeps the reference convention that every failure
+ * surfaces as a Python Exception (xgrid/util/logging.py:58-60).
+ *
+ * No torch or CUDA C++ types appear in the signatures: device memory is passed
+ * as plain pointers, CUDA streams as void*.
+ */
+#ifndef XGRID_GB300_H
+#define XGRID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XG_MAX_DIM 3
+#define XG_MAX_LEVELS 8
+
+/* Overstep modes (xgrid/util/init.py:48, xgrid/lang/generator.py:172-177). */
+#define XG_OVERSTEP_NONE 0
+#define XG_OVERSTEP_LIMIT 1
+#define XG_OVERSTEP_WRAP 2
+
+typedef struct xg_mask xg_mask;
+
+/*
+ * One grid argument.  Replaces the by-value C struct
+ *   struct __Grid<N>d_<T> { int32_t time; int32_t shape[N]; T** data; int32_t* boundary_mask; }
+ * that the reference passes to its generated C function
+ * (xgrid/lang/generator.py:144-165, xgrid/util/typing/reference.py:34-65,
+ *  serialised by xgrid/xgrid/__init__.py:60-68).
+ * Differences: level pointers and the scratch buffer are DEVICE pointers, the
+ * mask is a runtime handle with derived index tables, and the struct is passed
+ * by pointer so that the callee can report the level/scratch exchange of an
+ * in-place (Jacobi) sweep back to the caller.
+ */
+typedef struct xg_grid {
+    int32_t ndim;                  /* 1..XG_MAX_DIM                                  */
+    int32_t levels;                /* number of valid entries of level[] (the "time") */
+    int64_t shape[XG_MAX_DIM];     /* C-order extents, shape[ndim-1] is contiguous    */
+    void* level[XG_MAX_LEVELS];    /* level[0] = now, level[k] = k calls ago          */
+    void* scratch;                 /* device buffer of one level, exchanged with
+                                      level[0] by two-phase sweeps (may be NULL)      */
+    xg_mask* mask;                 /* boundary mask handle                            */
+} xg_grid;
+
+/*
+ * Entry point of a generated kernel module: runs the body of one
+ * @xgrid.kernel on `stream`.  Replaces the generated C function
+ *   <ret> <name>(struct __Grid.. g0, ..., scalars..., structs...)
+ * (xgrid/lang/generator.py:184-226) that Operator.__call__ invokes through
+ * Library.function (xgrid/lang/operator.py:29-41, xgrid/util/ffi.py:13-35).
+ * `grids` holds the grid arguments in declaration order, `args` the remaining
+ * arguments packed as a C struct in declaration order (natural alignment),
+ * `ret` receives the return value (nret bytes).  The call is asynchronous on
+ * `stream` except for kernels that return a value.
+ */
+typedef int (*xg_entry_fn)(xg_grid* grids, int ngrids, const void* args, size_t nargs,
+                           void* ret, size_t nret, void* stream);
+
+/* ---- errors -------------------------------------------------------------- */
+const char* xg_last_error(void);
+void xg_set_error(const char* message);
+int xg_runtime_version(void);
+
+/* ---- boundary masks ------------------------------------------------------ */
+/* Replaces Grid.boundary (xgrid/xgrid/__init__.py:40-41): an int32 array of the
+ * grid's shape whose value k selects the `with xgrid.boundary(k)` sweeps that
+ * update a cell (xgrid/lang/generator.py:295-298). */
+int xg_mask_create(int ndim, const int64_t* shape, xg_mask** out);
+int xg_mask_destroy(xg_mask* mask);
+/* Copy a host mask in, rebuild the per-value cell lists, upload (synchronous). */
+int xg_mask_upload(xg_mask* mask, const int32_t* host);
+uint64_t xg_mask_version(const xg_mask* mask);
+const int32_t* xg_mask_device(const xg_mask* mask);
+/* Device list of the cells (row-major linear indices, ascending) whose mask
+ * equals `value` (value != 0). */
+int xg_mask_cells(xg_mask* mask, int32_t value, const int64_t** cells, int64_t* count);
+/* Tile tables for a tiling of `tile` = {tz, ty, tx} cells (the last tile of
+ * each axis absorbs the remainder):  *tile_zero[t] = 1 when every cell of tile
+ * t has mask 0;  *csr_off/*csr_cells list the cells of mask `value` grouped by
+ * tile (csr_off has ntiles+1 entries).  Device pointers, owned by the mask. */
+int xg_mask_tiles(xg_mask* mask, const int32_t* tile, int32_t value,
+                  const uint8_t** tile_zero, const int32_t** csr_off,
+                  const int64_t** csr_cells, int64_t* ntiles);
+/* 1 in *ok when, for every cell c of mask `value` and each of the `noff`
+ * offsets (noff x 3, order z,y,x), the cell addressed from c under `overstep`
+ * lies in the same tile as c (reads outside the grid count as local). */
+int xg_mask_tile_local(xg_mask* mask, const int32_t* tile, int32_t value, int noff,
+                       const int32_t* offsets, int overstep, int* ok);
+
+/* ---- graph-cached calls -------------------------------------------------- */
+/* Call `fn` and cache the launches it makes as a CUDA graph keyed by the
+ * argument bytes and the grid pointers; later calls with the same key replay
+ * the graph and restore the level/scratch exchange and the return value.  The
+ * first call with a key runs eagerly (it may build mask tables).  use_graph = 0
+ * always calls eagerly. */
+int xg_call(xg_entry_fn fn, xg_grid* grids, int ngrids, const void* args, size_t nargs,
+            void* ret, size_t nret, void* stream, int use_graph);
+/* Drop every cached graph of `fn` (all when fn is NULL). */
+int xg_graph_clear(xg_entry_fn fn);
+int64_t xg_graph_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XGRID_GB300_H */

@@ -1,0 +1,133 @@
+"""DSL programs and seeded inputs of the benchmark configurations.
+
+Each kernel is ordinary ``@xgrid.kernel`` user code.  The diffusion and cavity
+bodies are written with the same expression trees, in the same order, as the
+reference's diffusion test case and examples/cavity.py:74-143 (51 Jacobi sweeps
+per step: one from the previous level, then 50 in place), because bit-for-bit
+parity depends on the order of floating-point operations.  Inputs are synthetic
+and seeded; they stand in for nothing external.
+"""
+import dataclasses
+
+import numpy as np
+
+import xgrid
+
+float2d = xgrid.grid[float, 2]
+float3d = xgrid.grid[float, 3]
+
+
+# ----------------------------------------------------------------- diffusion
+@xgrid.kernel()
+def diffusion2d(u: float2d, c: float) -> None:
+    """Explicit FTCS 5-point heat step, Dirichlet zero on mask 1."""
+    u[0, 0] = u[0, 0] + c * (u[1, 0] + u[-1, 0] + u[0, 1] + u[0, -1] - 4.0 * u[0, 0])
+    with xgrid.boundary(1):
+        u[0, 0] = 0.0
+
+
+def diffusion_setup(n: int = 512, seed: int = 0):
+    """512x512, u0 ~ U[0,1) from ``seed``, nu=0.1, dx=dy=1/(n-1), dt=0.2*dx^2/nu."""
+    nu = 0.1
+    dx = 1.0 / (n - 1)
+    dt = 0.2 * dx * dx / nu
+    c = nu * dt / (dx * dx)
+    u = xgrid.Grid((n, n), float)
+    u.now[...] = np.random.default_rng(seed).random((n, n))
+    b = u.boundary
+    b[0, :] = b[-1, :] = b[:, 0] = b[:, -1] = 1
+    return u, c
+
+
+# -------------------------------------------------------------------- cavity
+@dataclasses.dataclass
+class Config:
+    rho: float
+    nu: float
+    dt: float
+    dx: float
+    dy: float
+
+
+@xgrid.kernel()
+def cavity_kernel(b: float2d, p: float2d, u: float2d, v: float2d, cfg: Config) -> None:
+    b[0, 0] = (cfg.rho * (1.0 / cfg.dt *
+                          ((u[0, 1] - u[0, -1]) / (2.0 * cfg.dx) + (v[1, 0] - v[-1, 0]) / (2.0 * cfg.dy)) -
+                          ((u[0, 1] - u[0, -1]) / (2.0 * cfg.dx)) ** 2.0 -
+                          2.0 * ((u[1, 0] - u[-1, 0]) / (2.0 * cfg.dy) * (v[0, 1] - v[0, -1]) / (2.0 * cfg.dx)) -
+                          ((v[1, 0] - v[-1, 0]) / (2.0 * cfg.dy)) ** 2.0))
+
+    p[0, 0] = (((p[0, 1] + p[0, -1]) * cfg.dy ** 2.0 + (p[1, 0] + p[-1, 0]) * cfg.dx ** 2.0) /
+               (2.0 * (cfg.dx ** 2.0 + cfg.dy ** 2.0)) -
+               cfg.dx ** 2.0 * cfg.dy ** 2.0 / (2.0 * (cfg.dx ** 2.0 + cfg.dy ** 2.0)) * b[0, 0][0])
+    with xgrid.boundary(1):
+        p[0, 0] = p[0, -1][0]
+    with xgrid.boundary(2):
+        p[0, 0] = p[1, 0][0]
+    with xgrid.boundary(3):
+        p[0, 0] = p[0, 1][0]
+    with xgrid.boundary(4):
+        p[0, 0] = 0.0
+
+    for _ in range(0, 50):
+        p[0, 0] = (((p[0, 1][0] + p[0, -1][0]) * cfg.dy ** 2.0 + (p[1, 0][0] + p[-1, 0][0]) * cfg.dx ** 2.0) /
+                   (2.0 * (cfg.dx ** 2.0 + cfg.dy ** 2.0)) -
+                   cfg.dx ** 2.0 * cfg.dy ** 2.0 / (2.0 * (cfg.dx ** 2.0 + cfg.dy ** 2.0)) * b[0, 0][0])
+        with xgrid.boundary(1):
+            p[0, 0] = p[0, -1][0]
+        with xgrid.boundary(2):
+            p[0, 0] = p[1, 0][0]
+        with xgrid.boundary(3):
+            p[0, 0] = p[0, 1][0]
+        with xgrid.boundary(4):
+            p[0, 0] = 0.0
+
+    u[0, 0] = (u[0, 0] -
+               u[0, 0] * cfg.dt / cfg.dx * (u[0, 0] - u[0, -1]) -
+               v[0, 0] * cfg.dt / cfg.dy * (u[0, 0] - u[-1, 0]) -
+               cfg.dt / (2.0 * cfg.rho * cfg.dx) * (p[0, 1][0] - p[0, -1][0]) +
+               cfg.nu * (cfg.dt / cfg.dx ** 2.0 * (u[0, 1] - 2.0 * u[0, 0] + u[0, -1]) +
+                         cfg.dt / cfg.dy ** 2.0 * (u[1, 0] - 2.0 * u[0, 0] + u[-1, 0])))
+
+    v[0, 0] = (v[0, 0] -
+               u[0, 0] * cfg.dt / cfg.dx * (v[0, 0] - v[0, -1]) -
+               v[0, 0] * cfg.dt / cfg.dy * (v[0, 0] - v[-1, 0]) -
+               cfg.dt / (2.0 * cfg.rho * cfg.dy) * (p[1, 0][0] - p[-1, 0][0]) +
+               cfg.nu * (cfg.dt / cfg.dx ** 2.0 * (v[0, 1] - 2.0 * v[0, 0] + v[0, -1]) +
+                         cfg.dt / cfg.dy ** 2.0 * (v[1, 0] - 2.0 * v[0, 0] + v[-1, 0])))
+
+    with xgrid.boundary(1):
+        u[0, 0] = 0.0
+        v[0, 0] = 0.0
+    with xgrid.boundary(2):
+        u[0, 0] = 1.0
+
+
+def cavity_masks(n: int) -> dict:
+    """Boundary masks of the lid-driven cavity (same assignment order, hence the
+    same corner values, as the reference example)."""
+    m = {k: np.zeros((n, n), dtype=np.int32) for k in "bpuv"}
+    u = m["u"]
+    u[0, :] = 1
+    u[:, 0] = 1
+    u[:, -1] = 1
+    u[-1, :] = 2
+    m["v"].fill(1)
+    m["v"][1:-1, 1:-1] = 0
+    p = m["p"]
+    p[:, -1] = 1
+    p[0, :] = 2
+    p[:, 0] = 3
+    p[-1, :] = 4
+    m["b"].fill(1)
+    m["b"][1:-1, 1:-1] = 0
+    return m
+
+
+def cavity_setup(n: int = 1025, dt: float = 1e-5):
+    """Zero u, v, p, b on [0,2]^2 with n x n points, rho=1, nu=0.1."""
+    grids = {k: xgrid.Grid((n, n), float) for k in "bpuv"}
+    for k, mask in cavity_masks(n).items():
+        grids[k].boundary[...] = mask
+    cfg = Config(1.0, 0.1, dt, 2.0 / (n - 1), 2.0 / (n - 1))
+    return grids, cfg

@@ -1,0 +1,989 @@
+"""IR → CUDA (sm_103a) source for one ``@xgrid.kernel``.
+
+Replaces the reference's C/OpenMP generator (xgrid/lang/generator.py:79-442).
+The emitted module has
+
+* the user's dataclasses as C structs and every reachable ``@xgrid.function`` as
+  a ``__host__ __device__`` function (generator.py:144-165, 184-226, 405-419);
+* per launch group (see ``analysis``) one fused kernel plus one kernel per
+  sweep, built from three templates:
+    - main sweep: tiles of (tz, ty, tx) cells, one CTA per tile, each thread
+      walking the tile's cells; tiles whose cells all have mask 0 skip the mask
+      read, tiles whose neighbourhood lies inside the grid use unchecked
+      addressing; an implicit sweep writes the grid's scratch buffer (and copies
+      the cells it does not update) and the launcher exchanges scratch and
+      level 0 — the two-phase semantics of generator.py:312-352 without a
+      per-call malloc;
+    - boundary sweep: one thread per cell of the mask value's cell list instead
+      of a full-grid mask scan (generator.py:353-361);
+    - fused group: the main phase, then each boundary phase on the tile's own
+      boundary cells, separated by ``__syncthreads``;
+* a host entry ``xg_kernel_<name>`` that runs the body's control flow on the
+  CPU, evaluates every loop-invariant scalar subtree of a sweep once on the
+  host (the values the reference recomputes per cell; same IEEE operations, so
+  the results are identical) and launches the groups in program order;
+* kernels without grid arguments run their body in one device thread.
+
+Expressions keep the reference's C spelling and evaluation order: literals are
+C doubles (``repr(v).lower()``, generator.py:393-394), ``x ** 2.0`` becomes one
+multiplication (gcc folds ``pow(x, 2.0)`` that way; generator.py:377-383), other
+powers call ``pow``/``powf``.
+"""
+from __future__ import annotations
+
+import dataclasses
+import hashlib
+import math
+
+from . import analysis, ir
+from .config import Configuration
+from .log import Logger
+from .types import (Boolean, Floating, GridType, Ignore, Integer, Pointer, Structure, Value,
+                    Void)
+
+OVERSTEP = {"none": "XG_OVERSTEP_NONE", "limit": "XG_OVERSTEP_LIMIT", "wrap": "XG_OVERSTEP_WRAP"}
+
+# (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
+DEFAULT_TILING = {1: (1, 1, 256, 256, 1, 1), 2: (1, 8, 32, 32, 8, 1), 3: (1, 8, 32, 32, 8, 1)}
+
+_INT_RANK = {"bool": 0, "int8_t": 1, "int16_t": 2, "int": 3, "int32_t": 3, "int64_t": 4}
+
+
+def c_type(t) -> str:
+    if isinstance(t, Void):
+        return "void"
+    if isinstance(t, Boolean):
+        return "bool"
+    if isinstance(t, Integer):
+        return f"int{t.width_bits}_t"
+    if isinstance(t, Floating):
+        return "float" if t.width_bytes == 4 else "double"
+    if isinstance(t, Structure):
+        return f"struct {t.name}"
+    if isinstance(t, Pointer):
+        return c_type(t.element) + "*"
+    raise TypeError(f"type {t!r} has no C spelling")
+
+
+def arith(a: str, b: str) -> str:
+    """C usual arithmetic conversions for the types the DSL produces."""
+    if "double" in (a, b):
+        return "double"
+    if "float" in (a, b):
+        return "float"
+    ra, rb = _INT_RANK.get(a, 3), _INT_RANK.get(b, 3)
+    r = max(ra, rb, 3)
+    return "int64_t" if r == 4 else "int"
+
+
+def literal(value) -> str:
+    if isinstance(value, bool):
+        return "true" if value else "false"
+    if isinstance(value, float):
+        if math.isnan(value):
+            return "(0.0/0.0)"
+        if math.isinf(value):
+            return "(1.0/0.0)" if value > 0 else "(-1.0/0.0)"
+    return repr(value).lower()
+
+
+def pow_exponent(expr: ir.Expression):
+    """Exponent folded by gcc (2, 1, 0, -1), else None."""
+    if isinstance(expr, ir.Constant) and not isinstance(expr.value, bool) and expr.value in (2, 1, 0, -1):
+        return float(expr.value)
+    if isinstance(expr, ir.Unary) and expr.operator is ir.UnaryOperator.Neg and isinstance(expr.right, ir.Constant) \
+            and not isinstance(expr.right.value, bool) and expr.right.value == 1:
+        return -1.0
+    return None
+
+
+@dataclasses.dataclass
+class Module:
+    """What the Python side needs to call a generated module."""
+
+    source: str
+    name: str
+    entry: str
+    depth: int
+    grid_args: list          # [(name, GridType)]
+    value_args: list         # [(name, type)] in declaration order
+    arg_order: list          # ("grid"|"value", index) per declared argument
+    return_type: object
+    implicit_slots: list     # grid slots that need a scratch buffer
+    groups: int
+    device_only: bool        # kernel has no grid arguments (body runs on the device)
+    sweeps: list             # analysis.Sweep per grid assignment (for the oracle and tests)
+
+
+class CudaGenerator:
+    def __init__(self, operator, config: Configuration) -> None:
+        self.logger = Logger(self)
+        self.op = operator
+        self.cfg = config
+        self.defn: ir.Definition = operator.ir
+        self.structs: dict[str, Structure] = {}
+        self.functions: dict = {}       # id(func) -> (Operator, mangled)
+        self.function_order: list = []
+        self.device_chunks: list[str] = []
+        self.host_chunks: list[str] = []
+        self.depth = 0
+        self.group_counter = [0]
+        self.group_tiling: dict = {}
+        self.sweeps: list = []
+        self.slots = analysis.grid_slots(self.defn)
+        self.grid_names = {name: i for name, i in self.slots.items()}
+        self.mode = OVERSTEP[config.overstep]
+
+    # ================================================================ types
+    def use_type(self, t) -> str:
+        if isinstance(t, Structure):
+            if t.name not in self.structs:
+                for _, et in t.elements:
+                    self.use_type(et)
+                self.structs[t.name] = t
+        elif isinstance(t, Pointer):
+            self.use_type(t.element)
+        return c_type(t)
+
+    def ctype(self, e: ir.Expression) -> str:
+        """C type of an expression as gcc would type the reference's C."""
+        if isinstance(e, ir.Constant):
+            if isinstance(e.value, bool):
+                return "int"
+            return "int" if isinstance(e.value, int) else "double"
+        if isinstance(e, (ir.Identifier, ir.Stencil, ir.Access, ir.Call, ir.Cast)):
+            return self.use_type(e.type)
+        if isinstance(e, ir.GridInfo):
+            return "int"
+        if isinstance(e, ir.Unary):
+            if e.operator is ir.UnaryOperator.Not:
+                return "int"
+            return arith(self.ctype(e.right), "int")
+        if isinstance(e, ir.Condition):
+            a, b = self.ctype(e.body), self.ctype(e.orelse)
+            return a if a == b else arith(a, b)
+        if isinstance(e, ir.Binary):
+            if e.operator.is_compare() or e.operator.is_logic():
+                return "int"
+            if e.operator is ir.BinaryOperator.Pow:
+                return "double" if (isinstance(e.type, Floating) and e.type.width_bits == 64) else "float"
+            return arith(self.ctype(e.left), self.ctype(e.right))
+        raise TypeError(f"cannot type {type(e).__name__}")
+
+    # ========================================================== expressions
+    def expr(self, e: ir.Expression, env) -> str:
+        """C source of an expression.  ``env`` resolves stencils, hoisted subtrees
+        and grid info (host or device context)."""
+        sub = env.substitute(e)
+        if sub is not None:
+            return sub
+        if isinstance(e, ir.Constant):
+            return literal(e.value)
+        if isinstance(e, ir.Identifier):
+            if isinstance(e.variable.type, Pointer):
+                return f"(*{e.variable.name})"
+            return e.variable.name
+        if isinstance(e, ir.Stencil):
+            return env.stencil(e)
+        if isinstance(e, ir.Access):
+            return f"({self.expr(e.value, env)}).{e.attribute}"
+        if isinstance(e, ir.Unary):
+            return f"({e.operator.value} {self.expr(e.right, env)})"
+        if isinstance(e, ir.Condition):
+            return f"({self.expr(e.condition, env)} ? {self.expr(e.body, env)} : {self.expr(e.orelse, env)})"
+        if isinstance(e, ir.Cast):
+            return f"(({self.use_type(e.type)})({self.expr(e.value, env)}))"
+        if isinstance(e, ir.GridInfo):
+            return env.grid_info(e, self)
+        if isinstance(e, ir.Binary):
+            if e.operator is ir.BinaryOperator.Pow:
+                double = isinstance(e.type, Floating) and e.type.width_bits == 64
+                k = pow_exponent(e.right)
+                base = self.expr(e.left, env)
+                t = "double" if double else "float"
+                if k == 2.0:
+                    return f"xg_sq_{'d' if double else 'f'}(({t})({base}))"
+                if k == 1.0:
+                    return f"(({t})({base}))"
+                if k == 0.0:
+                    return f"(({t})1)"
+                if k == -1.0:
+                    return f"(({t})1 / ({t})({base}))"
+                return f"{'pow' if double else 'powf'}({base}, {self.expr(e.right, env)})"
+            if e.operator is ir.BinaryOperator.Mod and "int" not in self.ctype(e):
+                self.logger.dead("Operator '%' requires integer operands in C")
+            return f"({self.expr(e.left, env)} {e.operator.value} {self.expr(e.right, env)})"
+        if isinstance(e, ir.Call):
+            return self.call(e, env)
+        raise TypeError(f"cannot emit {type(e).__name__}")
+
+    def call(self, e: ir.Call, env) -> str:
+        from .operator import Operator
+        args = []
+        for i, a in enumerate(e.arguments):
+            code = self.expr(a, env)
+            at = e.operator.signature.arguments[i][1]
+            if isinstance(at, Pointer) and a.type == at.element:
+                code = f"&{code}"
+            args.append(code)
+        if isinstance(e.operator, ir.Constructor):
+            self.use_type(e.operator.type)
+            return f"xg_make_{e.operator.type.name}({', '.join(args)})"
+        op: Operator = e.operator
+        if op.mode == "external":
+            if op.name in ("tick",):
+                self.logger.dead(f"External operator '{op.name}' has no implementation")
+            if env.device:
+                self.logger.dead(f"External operator '{op.name}' cannot be called inside a grid sweep on the GPU")
+            return f"{op.name}({', '.join(args)})"
+        return f"{self.function(op)}({', '.join(args)})"
+
+    def function(self, op) -> str:
+        key = (op.func, op.self_type.name if op.self_type is not None else None, op.name)
+        if key in self.functions:
+            return self.functions[key][1]
+        mangled = f"xgf_{op.self_type.name}_{op.name}" if op.self_type is not None else f"xgf_{op.name}"
+        used = {v[1] for v in self.functions.values()}
+        base, n = mangled, 1
+        while mangled in used:
+            mangled = f"{base}_{n}"
+            n += 1
+        self.functions[key] = (op, mangled)
+        self.function_order.append(key)
+        defn = op.ir
+        for name, t in defn.signature.arguments:
+            if isinstance(t, GridType):
+                self.logger.dead(f"Function '{op.name}' takes a grid argument; only kernels may sweep grids")
+        return mangled
+
+    # ============================================================ statements
+    def block(self, stmts: list, env, indent: str, out: list, ret_mode: str) -> None:
+        """Emit a statement list (host entry or device function body)."""
+        i = 0
+        while i < len(stmts):
+            s = stmts[i]
+            if isinstance(s, ir.Assignment) and isinstance(s.terminal, ir.Stencil):
+                run = []
+                while i < len(stmts) and isinstance(stmts[i], ir.Assignment) and isinstance(stmts[i].terminal, ir.Stencil):
+                    run.append(stmts[i])
+                    i += 1
+                if env.device:
+                    self.logger.dead("Grid sweeps are only allowed in kernels")
+                self.emit_run(run, env, indent, out)
+                continue
+            i += 1
+            if self.cfg.comment:
+                out.append(f'#line {s.location.line} "{s.location.file}"')
+            if isinstance(s, ir.Assignment):
+                out.append(f"{indent}{self.expr(s.terminal, env)} = {self.expr(s.value, env)};")
+            elif isinstance(s, ir.Return):
+                out.extend(env.ret(self, s, indent))
+            elif isinstance(s, ir.Break):
+                out.append(f"{indent}break;")
+            elif isinstance(s, ir.Continue):
+                out.append(f"{indent}continue;")
+            elif isinstance(s, ir.Evaluation):
+                out.append(f"{indent}{self.expr(s.value, env)};")
+            elif isinstance(s, ir.Inline):
+                out.append(s.source)
+            elif isinstance(s, ir.If):
+                out.append(f"{indent}if ({self.expr(s.condition, env)}) {{")
+                self.block(s.body, env, indent + "  ", out, ret_mode)
+                if s.orelse:
+                    out.append(f"{indent}}} else {{")
+                    self.block(s.orelse, env, indent + "  ", out, ret_mode)
+                out.append(f"{indent}}}")
+            elif isinstance(s, ir.While):
+                out.append(f"{indent}while ({self.expr(s.condition, env)}) {{")
+                self.block(s.body, env, indent + "  ", out, ret_mode)
+                out.append(f"{indent}}}")
+            elif isinstance(s, ir.For):
+                v = s.variable.name
+                out.append(f"{indent}for ({v} = {self.expr(s.start, env)}; {v} < {self.expr(s.end, env)}; "
+                           f"{v} += {self.expr(s.step, env)}) {{")
+                self.block(s.body, env, indent + "  ", out, ret_mode)
+                out.append(f"{indent}}}")
+            else:
+                raise TypeError(f"cannot emit statement {type(s).__name__}")
+
+    # ================================================================ sweeps
+    def emit_run(self, run: list, env, indent: str, out: list) -> None:
+        sweeps = [analysis.collect_sweep(s, self.slots, self.logger) for s in run]
+        for s in sweeps:
+            for st, _ in s.loads:
+                self.depth = max(self.depth, abs(st.time_offset))
+            self.depth = max(self.depth, s.level)
+        self.sweeps.extend(sweeps)
+        groups = analysis.build_groups(sweeps, self.group_counter, self.cfg.fuse)
+        for g in groups:
+            dim = self.defn.signature.arguments[SweepGroupEmitter(self, g).arg_index(g.sweeps[0].slot)][1].dimension
+            self.group_tiling[g.index] = DEFAULT_TILING[dim]
+            SweepGroupEmitter(self, g).emit(env, indent, out)
+
+    # ================================================================ module
+    def generate(self) -> Module:
+        d = self.defn
+        analysis.check_loads(d.body, self.logger)
+        grid_args, value_args, order = [], [], []
+        for name, t in d.signature.arguments:
+            if isinstance(t, GridType):
+                if d.signature.arguments and t.dimension not in (1, 2, 3):
+                    self.logger.dead(f"Grid '{name}' has {t.dimension} dimensions; 1 to 3 are supported")
+                self.use_type(t.element)
+                order.append(("grid", len(grid_args)))
+                grid_args.append((name, t))
+            else:
+                if isinstance(t, Ignore):
+                    self.logger.dead(f"Argument '{name}' of a kernel needs a concrete type")
+                self.use_type(t)
+                order.append(("value", len(value_args)))
+                value_args.append((name, t))
+        rtype = d.signature.return_type
+        self.use_type(rtype)
+        device_only = not grid_args
+        name = self.op.name
+        entry = f"xg_kernel_{name}"
+
+        body: list[str] = []
+        if device_only:
+            env = DeviceScalarEnv(self)
+            body_lines: list[str] = []
+            self.block(d.body, env, "  ", body_lines, "device")
+            self.device_chunks.append(self.scalar_kernel(name, value_args, rtype, d, body_lines))
+            body.extend(self.scalar_entry(name, entry, value_args, rtype))
+        else:
+            env = HostEnv(self)
+            lines: list[str] = []
+            self.block(d.body, env, "  ", lines, "host")
+            body.extend(self.host_entry(name, entry, value_args, rtype, d, lines))
+
+        src: list[str] = ['#include "xgrid_gen.cuh"']
+        for inc in self.op.includes:
+            src.append(f'#include "{inc}"')
+        src.append("")
+        fn_protos, fn_defs = self.function_defs()
+        src.extend(self.struct_defs())
+        src.extend(fn_protos)
+        src.extend(fn_defs)
+        src.append(f"static const int xg_overstep = {self.mode};")
+        src.append(f"struct xga_{name} {{")
+        for an, at in value_args:
+            src.append(f"  {c_type(at)} {an};")
+        if not value_args:
+            src.append("  char xg_empty;")
+        src.append("};")
+        src.append(f"static int xg_fuse_{name} = {1 if self.cfg.fuse else 0};")
+        src.append(f"static int32_t xg_tiling_{name}[{max(self.group_counter[0], 1)}][6] = {{")
+        for gi in range(max(self.group_counter[0], 1)):
+            src.append("  {" + ", ".join(str(v) for v in self.group_tiling.get(gi, DEFAULT_TILING[2])) + "},")
+        src.append("};")
+        src.extend(self.device_chunks)
+        src.extend(self.host_chunks)
+        src.extend(body)
+        src.append(f'extern "C" int xg_config_{name}(int group, const int32_t* cfg, int fuse) {{')
+        src.append(f"  if (fuse >= 0) xg_fuse_{name} = fuse;")
+        src.append(f"  if (group < 0 || group >= {self.group_counter[0]} || !cfg) return 0;")
+        src.append(f"  for (int i = 0; i < 6; ++i) xg_tiling_{name}[group][i] = cfg[i];")
+        src.append("  return 0;")
+        src.append("}")
+        src.append(f'extern "C" int xg_groups_{name}(void) {{ return {self.group_counter[0]}; }}')
+        implicit = sorted({s.slot for s in self.sweeps if s.implicit})
+        return Module("\n".join(src) + "\n", name, entry, self.depth + 1, grid_args, value_args, order, rtype,
+                      implicit, self.group_counter[0], device_only, self.sweeps)
+
+    def struct_defs(self) -> list[str]:
+        out = []
+        for s in self.structs.values():
+            out.append(f"struct {s.name} {{")
+            for n, t in s.elements:
+                out.append(f"  {c_type(t)} {n};")
+            out.append("};")
+            params = ", ".join(f"{c_type(t)} {n}" for n, t in s.elements)
+            fields = "; ".join(f"v.{n} = {n}" for n, _ in s.elements)
+            out.append(f"XG_HD struct {s.name} xg_make_{s.name}({params}) {{ struct {s.name} v; {fields}; return v; }}")
+        return out
+
+    def function_defs(self):
+        protos, defs = [], []
+        done = 0
+        while done < len(self.function_order):
+            key = self.function_order[done]
+            done += 1
+            op, mangled = self.functions[key]
+            d = op.ir
+            rt = self.use_type(d.signature.return_type)
+            params = ", ".join(f"{self.use_type(t)} {n}" for n, t in d.signature.arguments)
+            proto = f"static __host__ __device__ {rt} {mangled}({params})"
+            protos.append(proto + ";")
+            lines = [proto + " {"]
+            for vn, var in d.scope.items():
+                if vn not in d.signature.argnames_map:
+                    lines.append(f"  {self.use_type(var.type)} {vn};")
+            for m in op.macro:
+                lines.append(m)
+            env = FunctionEnv(self)
+            self.block(d.body, env, "  ", lines, "function")
+            lines.append("}")
+            defs.extend(lines)
+        # struct definitions may have grown while emitting functions; they are
+        # written before the prototypes, so nothing else to do here.
+        return protos, defs
+
+    def scalar_kernel(self, name, value_args, rtype, d, body_lines) -> str:
+        rt = c_type(rtype)
+        out = []
+        if not isinstance(rtype, Void):
+            out.append(f"static __device__ {rt} xg_ret_{name};")
+        out.append(f"__global__ void xgk_{name}_scalar(struct xga_{name} xg_a) {{")
+        for an, at in value_args:
+            out.append(f"  {c_type(at)} {an} = xg_a.{an};")
+        for vn, var in d.scope.items():
+            if vn not in d.signature.argnames_map:
+                out.append(f"  {self.use_type(var.type)} {vn};")
+        for m in self.op.macro:
+            out.append(m)
+        out.extend(body_lines)
+        out.append("}")
+        return "\n".join(out)
+
+    def scalar_entry(self, name, entry, value_args, rtype) -> list[str]:
+        rt = c_type(rtype)
+        out = [f'extern "C" int {entry}(xg_grid* G, int ngrids, const void* args, size_t nargs, void* ret, '
+               f'size_t nret, void* stream) {{',
+               "  (void)G; (void)ngrids;",
+               "  cudaStream_t s = (cudaStream_t)stream;",
+               f"  struct xga_{name} a;",
+               f"  if (nargs != {'sizeof(a)' if value_args else '0'}) XG_FAIL(\"{name}: argument block has %zu bytes, "
+               f"expected %zu\", nargs, (size_t){'sizeof(a)' if value_args else '0'});",
+               "  memset(&a, 0, sizeof a);",
+               "  if (nargs) memcpy(&a, args, nargs);",
+               f"  xgk_{name}_scalar<<<1, 1, 0, s>>>(a);",
+               "  XG_CUDA(cudaGetLastError());"]
+        if not isinstance(rtype, Void):
+            out += [f"  if (!ret || nret != sizeof({rt})) XG_FAIL(\"{name}: return buffer has %zu bytes\", nret);",
+                    f"  XG_CUDA(cudaMemcpyFromSymbolAsync(ret, xg_ret_{name}, sizeof({rt}), 0, "
+                    f"cudaMemcpyDeviceToHost, s));",
+                    "  XG_CUDA(cudaStreamSynchronize(s));"]
+        out += ["  return 0;", "}"]
+        return out
+
+    def host_entry(self, name, entry, value_args, rtype, d, lines) -> list[str]:
+        out = [f'extern "C" int {entry}(xg_grid* G, int ngrids, const void* args, size_t nargs, void* ret, '
+               f'size_t nret, void* stream) {{',
+               "  cudaStream_t s = (cudaStream_t)stream;",
+               f"  if (ngrids != {len(self.slots)}) XG_FAIL(\"{name}: expected {len(self.slots)} grids, got %d\", ngrids);",
+               f"  struct xga_{name} a;",
+               f"  if (nargs != {'sizeof(a)' if value_args else '0'}) XG_FAIL(\"{name}: argument block has %zu bytes, "
+               f"expected %zu\", nargs, (size_t){'sizeof(a)' if value_args else '0'});",
+               "  memset(&a, 0, sizeof a);",
+               "  if (nargs) memcpy(&a, args, nargs);",
+               "  (void)ret; (void)nret; (void)s;"]
+        for an, at in value_args:
+            out.append(f"  {c_type(at)} {an} = a.{an};")
+        for vn, var in d.scope.items():
+            if vn not in d.signature.argnames_map:
+                out.append(f"  {self.use_type(var.type)} {vn};")
+        for m in self.op.macro:
+            out.append(m)
+        out.extend(lines)
+        out += ["  return 0;", "}"]
+        return out
+
+
+# ==================================================================== envs
+class HostEnv:
+    device = False
+
+    def __init__(self, gen: CudaGenerator) -> None:
+        self.gen = gen
+
+    def substitute(self, e):
+        return None
+
+    def stencil(self, e):
+        self.gen.logger.dead(f"Unable to perform load operation to grid '{e.variable.name}' without stencil context")
+
+    def grid_info(self, e: ir.GridInfo, gen) -> str:
+        slot = gen.slots[e.variable.name]
+        if e.info == "dimension":
+            return str(e.variable.type.dimension)
+        return f"((int32_t)G[{slot}].shape[{gen.expr(e.dimension, self)}])"
+
+    def ret(self, gen, s: ir.Return, indent: str) -> list[str]:
+        if s.value is None:
+            return [f"{indent}return 0;"]
+        t = c_type(s.value.type)
+        return [f"{indent}{{ {t} r_ = {gen.expr(s.value, self)};",
+                f"{indent}  if (ret && nret == sizeof r_) memcpy(ret, &r_, sizeof r_);",
+                f"{indent}  return 0; }}"]
+
+
+class FunctionEnv(HostEnv):
+    device = False
+
+    def ret(self, gen, s, indent):
+        if s.value is None:
+            return [f"{indent}return;"]
+        return [f"{indent}return {gen.expr(s.value, self)};"]
+
+    def grid_info(self, e, gen):
+        gen.logger.dead("shape/dimension need a grid argument of a kernel")
+
+
+class DeviceScalarEnv(FunctionEnv):
+    """Body of a kernel without grids, run by one device thread."""
+
+    device = True
+
+    def ret(self, gen, s, indent):
+        if s.value is None:
+            return [f"{indent}return;"]
+        return [f"{indent}{{ xg_ret_{gen.op.name} = {gen.expr(s.value, self)}; return; }}"]
+
+
+@dataclasses.dataclass
+class Hoisted:
+    name: str
+    ctype: str
+    expr: ir.Expression
+
+
+class SweepEnv:
+    """Device context of one sweep: stencils → preloaded locals, hoisted subtrees
+    → kernel parameters."""
+
+    device = True
+
+    def __init__(self, gen, hoisted: dict, loadnames: dict) -> None:
+        self.gen = gen
+        self.hoisted = hoisted
+        self.loadnames = loadnames
+
+    def substitute(self, e):
+        h = self.hoisted.get(id(e))
+        return f"p.h.{h.name}" if h is not None else None
+
+    def stencil(self, e):
+        return self.loadnames[id(e)]
+
+    def grid_info(self, e, gen):
+        raise AssertionError("grid info is always hoisted")
+
+
+def has_stencil(e) -> bool:
+    return any(isinstance(n, ir.Stencil) for n in ir.walk(e))
+
+
+def unsafe_int_div(e) -> bool:
+    return any(isinstance(n, ir.Binary) and n.operator in (ir.BinaryOperator.Div, ir.BinaryOperator.Mod)
+               and isinstance(n.type, Integer) for n in ir.walk(e))
+
+
+class SweepGroupEmitter:
+    """Kernels and launchers of one launch group."""
+
+    def __init__(self, gen: CudaGenerator, group: analysis.Group) -> None:
+        self.gen = gen
+        self.g = group
+        self.name = gen.op.name
+        self.gid = group.index
+        self.hoisted: list[Hoisted] = []
+        self.hoist_map: dict = {}
+
+    # ---------------------------------------------------------- hoisting
+    def hoist(self, e: ir.Expression, conditional: bool = False) -> None:
+        """Hoist maximal stencil-free subtrees (not bare constants)."""
+        if not has_stencil(e):
+            if isinstance(e, ir.Constant):
+                return
+            if conditional and unsafe_int_div(e):
+                pass  # an integer division guarded by a condition stays per cell
+            else:
+                h = Hoisted(f"v{len(self.hoisted)}", self.gen.ctype(e), e)
+                self.hoisted.append(h)
+                self.hoist_map[id(e)] = h
+                return
+        if isinstance(e, ir.Binary):
+            cond = conditional or e.operator.is_logic()
+            self.hoist(e.left, conditional)
+            self.hoist(e.right, cond)
+        elif isinstance(e, ir.Unary):
+            self.hoist(e.right, conditional)
+        elif isinstance(e, ir.Condition):
+            self.hoist(e.condition, conditional)
+            self.hoist(e.body, True)
+            self.hoist(e.orelse, True)
+        elif isinstance(e, ir.Cast):
+            self.hoist(e.value, conditional)
+        elif isinstance(e, ir.Access):
+            self.hoist(e.value, conditional)
+        elif isinstance(e, ir.Call):
+            for a in e.arguments:
+                self.hoist(a, conditional)
+
+    # ----------------------------------------------------------- emission
+    def emit(self, env: HostEnv, indent: str, out: list) -> None:
+        gen = self.gen
+        for s in self.g.sweeps:
+            self.hoist(s.stmt.value)
+        n = self.name
+        gid = self.gid
+        # hoisted values struct + their host evaluation
+        hs = [f"struct xgh_{n}_{gid} {{"]
+        for h in self.hoisted:
+            hs.append(f"  {h.ctype} {h.name};")
+        if not self.hoisted:
+            hs.append("  char xg_empty;")
+        hs.append("};")
+        gen.device_chunks.append("\n".join(hs))
+        out.append(f"{indent}{{ struct xgh_{n}_{gid} h_;")
+        out.append(f"{indent}  memset(&h_, 0, sizeof h_);")
+        for h in self.hoisted:
+            out.append(f"{indent}  h_.{h.name} = {gen.expr(h.expr, env)};")
+        out.append(f"{indent}  XG_TRY(xgl_{n}_{gid}(G, &h_, s)); }}")
+
+        launchers = []
+        if self.g.fusable:
+            self.emit_fused()
+            launchers.append("fused")
+        for j, s in enumerate(self.g.sweeps):
+            if s.is_main:
+                self.emit_main_single(j, s)
+            else:
+                self.emit_bnd_single(j, s)
+        # dispatcher
+        lines = [f"static int xgl_{n}_{gid}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s) {{"]
+        if self.g.fusable:
+            lines += [f"  if (xg_fuse_{n}) {{",
+                      f"    int r = xgl_{n}_{gid}_fused(G, h, s);",
+                      "    if (r < 0) return r;",
+                      "    if (r > 0) return 0;",
+                      "  }"]
+        for j, _ in enumerate(self.g.sweeps):
+            lines.append(f"  XG_TRY(xgl_{n}_{gid}_s{j}(G, h, s));")
+        lines += ["  return 0;", "}"]
+        gen.host_chunks.append("\n".join(lines))
+
+    # ------------------------------------------------------------ helpers
+    def elem(self, slot: int) -> str:
+        return c_type(self.gen.defn.signature.arguments[self.arg_index(slot)][1].element)
+
+    def arg_index(self, slot: int) -> int:
+        k = -1
+        for i, (_, t) in enumerate(self.gen.defn.signature.arguments):
+            if isinstance(t, GridType):
+                k += 1
+                if k == slot:
+                    return i
+        raise IndexError(slot)
+
+    def buffers(self, sweeps) -> list:
+        """Distinct (slot, level, version) buffers read or written by ``sweeps``."""
+        bufs = []
+        for s in sweeps:
+            for _, ld in s.loads:
+                b = (ld.slot, ld.level, ld.version)
+                if b not in bufs:
+                    bufs.append(b)
+            for b in [(s.slot, s.level, s.read_version_of_target), (s.slot, s.level, s.write_version)]:
+                if b not in bufs:
+                    bufs.append(b)
+        return bufs
+
+    @staticmethod
+    def bname(b) -> str:
+        return f"b{b[0]}_{b[1]}_{b[2]}"
+
+    def buffer_ptr_host(self, b, single) -> str:
+        """Host expression of a buffer pointer before this launch's exchanges.
+
+        Fused launch: version 0 is the level pointer, version 1 the scratch buffer
+        that an implicit sweep of the group writes.  Single-sweep launch (``single``
+        is that sweep): every earlier exchange has already happened, so every
+        buffer is the current level pointer except the write of an implicit sweep.
+        """
+        slot, level, version = b
+        if single is not None:
+            if single.implicit and b == (single.slot, single.level, single.write_version):
+                return f"G[{slot}].scratch"
+            return f"G[{slot}].level[{level}]"
+        if version == 0:
+            return f"G[{slot}].level[{level}]"
+        return f"G[{slot}].scratch"
+
+    def slots_used(self, sweeps) -> list:
+        out = []
+        for b in self.buffers(sweeps):
+            if b[0] not in out:
+                out.append(b[0])
+        return out
+
+    def params_struct(self, tag: str, sweeps, extra: list) -> str:
+        n, gid = self.name, self.gid
+        lines = [f"struct xgp_{n}_{gid}_{tag} {{", f"  struct xgh_{n}_{gid} h;",
+                 "  int64_t Z, Y, X;", "  int32_t tz, ty, tx;", "  int64_t ntz, nty, ntx;", "  int same;"]
+        for b in self.buffers(sweeps):
+            lines.append(f"  {self.elem(b[0])}* {self.bname(b)};")
+        for slot in self.slots_used(sweeps):
+            lines.append(f"  int64_t e{slot}[3];")
+        lines.extend(f"  {x};" for x in extra)
+        lines.append("};")
+        return "\n".join(lines)
+
+    def load_code(self, sweep, ld: analysis.Load, fast: bool) -> str:
+        b = self.bname((ld.slot, ld.level, ld.version))
+        oz, oy, ox = ld.offset
+        if fast:
+            off = []
+            if oz:
+                off.append(f"({oz}) * sz")
+            if oy:
+                off.append(f"({oy}) * sy")
+            if ox:
+                off.append(f"({ox})")
+            idx = "c" + "".join(f" + {o}" for o in off)
+            return f"p.{b}[{idx}]"
+        e = f"p.e{ld.slot}"
+        return (f"xg_ldc(p.{b}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, {e}[0], {e}[1], {e}[2]))")
+
+    def value_code(self, sweep, fast: bool, indent: str) -> tuple[list, str]:
+        """Preload lines and the value expression of a sweep at cell (z,y,x)=c."""
+        lines, names = [], {}
+        local = {}
+        for st, ld in sweep.loads:
+            if ld not in local:
+                vn = f"l{len(local)}"
+                local[ld] = vn
+                lines.append(f"{indent}const {self.elem(ld.slot)} {vn} = {self.load_code(sweep, ld, fast)};")
+            names[id(st)] = local[ld]
+        env = SweepEnv(self.gen, self.hoist_map, names)
+        return lines, self.gen.expr(sweep.stmt.value, env)
+
+    def main_body(self, sweeps_idx: list, fast: bool, indent: str, mask_vars: dict) -> list:
+        lines = []
+        for j in sweeps_idx:
+            s = self.g.sweeps[j]
+            dst = self.bname((s.slot, s.level, s.write_version))
+            src = self.bname((s.slot, s.level, s.read_version_of_target))
+            pre, val = self.value_code(s, fast, indent + "  ")
+            cond = f"{mask_vars[j]} || p.m{j}[c] == 0"
+            lines.append(f"{indent}if ({cond}) {{")
+            lines.extend(pre)
+            if any(s.store_offset):
+                oz, oy, ox = s.store_offset
+                e = f"p.e{s.slot}"
+                lines.append(f"{indent}  xg_stc(p.{dst}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, "
+                             f"{e}[0], {e}[1], {e}[2]), ({self.elem(s.slot)})({val}));")
+            else:
+                lines.append(f"{indent}  p.{dst}[c] = {val};")
+            if s.implicit and not any(s.store_offset):
+                lines.append(f"{indent}}} else {{")
+                lines.append(f"{indent}  p.{dst}[c] = p.{src}[c];")
+            lines.append(f"{indent}}}")
+        return lines
+
+    def main_kernel(self, tag: str, mains: list, bnd_phases: list) -> str:
+        """Tile kernel: main sweeps ``mains`` (indices into the group) then the
+        boundary phases ``bnd_phases`` on the tile's own cells."""
+        n, gid = self.name, self.gid
+        sweeps = [self.g.sweeps[j] for j in mains]
+        # neighbourhood of the main loads, for the unchecked fast path
+        lo = [0, 0, 0]
+        hi = [0, 0, 0]
+        for s in sweeps:
+            for _, ld in s.loads:
+                for a in range(3):
+                    lo[a] = min(lo[a], ld.offset[a])
+                    hi[a] = max(hi[a], ld.offset[a])
+        lines = [f"__global__ void __launch_bounds__(1024) xgk_{n}_{gid}_{tag}(const __grid_constant__ "
+                 f"struct xgp_{n}_{gid}_{tag} p) {{",
+                 "  const int64_t t = blockIdx.x;",
+                 "  const int64_t itx = t % p.ntx, ity = (t / p.ntx) % p.nty, itz = t / (p.ntx * p.nty);",
+                 "  int64_t z0, z1, y0, y1, x0, x1;",
+                 "  xg_tile_range(p.Z, p.tz, p.ntz, itz, &z0, &z1);",
+                 "  xg_tile_range(p.Y, p.ty, p.nty, ity, &y0, &y1);",
+                 "  xg_tile_range(p.X, p.tx, p.ntx, itx, &x0, &x1);",
+                 "  const int64_t sy = p.X, sz = p.X * p.Y;",
+                 "  (void)sy; (void)sz;",
+                 f"  const bool fast = p.same && z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && "
+                 f"y0 + ({lo[1]}) >= 0 && y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;"]
+        mask_vars = {}
+        for j in mains:
+            mask_vars[j] = f"mz{j}"
+            lines.append(f"  const bool mz{j} = p.tzero{j}[t] != 0;")
+        loop_head = ["  for (int64_t z = z0; z < z1; ++z)",
+                     "  for (int64_t y = y0 + threadIdx.y; y < y1; y += blockDim.y)",
+                     "  for (int64_t x = x0 + threadIdx.x; x < x1; x += blockDim.x) {",
+                     "    const int64_t c = (z * p.Y + y) * p.X + x;"]
+        lines.append("  if (fast) {")
+        lines += ["  " + l for l in loop_head]
+        lines += self.main_body(mains, True, "      ", mask_vars)
+        lines.append("    }")
+        lines.append("  } else {")
+        lines += ["  " + l for l in loop_head]
+        lines += self.main_body(mains, False, "      ", mask_vars)
+        lines.append("    }")
+        lines.append("  }")
+        for j in bnd_phases:
+            s = self.g.sweeps[j]
+            dst = self.bname((s.slot, s.level, s.write_version))
+            pre, val = self.value_code(s, False, "    ")
+            lines += ["  __syncthreads();",
+                      "  {",
+                      "    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);",
+                      "    const int nthr = blockDim.x * blockDim.y * blockDim.z;",
+                      f"    for (int64_t e = p.bo{j}[t] + tid; e < p.bo{j}[t + 1]; e += nthr) {{",
+                      f"    const int64_t c = p.bc{j}[e];",
+                      f"    const int64_t x = c % p.e{s.slot}[2], y = (c / p.e{s.slot}[2]) % p.e{s.slot}[1], "
+                      f"z = c / (p.e{s.slot}[2] * p.e{s.slot}[1]);",
+                      "    (void)x; (void)y; (void)z;"]
+            lines += pre
+            lines.append(f"    p.{dst}[c] = {val};")
+            lines += ["    }", "  }"]
+        lines.append("}")
+        return "\n".join(lines)
+
+    def fill_params(self, tag: str, sweeps, dom_slot: int, single=None, indent: str = "  ") -> list:
+        n, gid = self.name, self.gid
+        lines = [f"{indent}struct xgp_{n}_{gid}_{tag} p;",
+                 f"{indent}memset(&p, 0, sizeof p);",
+                 f"{indent}p.h = *h;",
+                 f"{indent}const int32_t* tl = xg_tiling_{n}[{gid}];",
+                 f"{indent}xg_ext dom = xg_extent(&G[{dom_slot}]);",
+                 f"{indent}p.Z = dom.z; p.Y = dom.y; p.X = dom.x;",
+                 f"{indent}p.tz = tl[0]; p.ty = tl[1]; p.tx = tl[2];",
+                 f"{indent}p.ntz = xg_tiles_along(p.Z, p.tz); p.nty = xg_tiles_along(p.Y, p.ty); "
+                 f"p.ntx = xg_tiles_along(p.X, p.tx);",
+                 f"{indent}p.same = 1;"]
+        for slot in self.slots_used(sweeps):
+            lines += [f"{indent}{{ xg_ext e = xg_extent(&G[{slot}]); p.e{slot}[0] = e.z; p.e{slot}[1] = e.y; "
+                      f"p.e{slot}[2] = e.x; if (!xg_same_ext(e, dom)) p.same = 0; }}"]
+        for b in self.buffers(sweeps):
+            lines.append(f"{indent}p.{self.bname(b)} = ({self.elem(b[0])}*){self.buffer_ptr_host(b, single)};")
+        return lines
+
+    def check_levels(self, sweeps, single=None, indent="  ") -> list:
+        lines = []
+        for b in self.buffers(sweeps):
+            slot, level, version = b
+            lines.append(f"{indent}if (G[{slot}].levels <= {level}) XG_FAIL(\"{self.name}: grid argument {slot} "
+                         f"has %d time levels, level {level} is read\", G[{slot}].levels);")
+            if "scratch" in self.buffer_ptr_host(b, single):
+                lines.append(f"{indent}if (!G[{slot}].scratch) XG_FAIL(\"{self.name}: grid argument {slot} "
+                             f"has no scratch buffer\");")
+        return lines
+
+    def emit_main_single(self, j: int, s) -> None:
+        n, gid = self.name, self.gid
+        tag = f"s{j}"
+        sweeps = [s]
+        extra = [f"const int32_t* m{j}", f"const uint8_t* tzero{j}"]
+        self.gen.device_chunks.append(self.params_struct(tag, sweeps, extra))
+        implicit_scatter = s.implicit and any(s.store_offset)
+        self.gen.device_chunks.append(self.main_kernel(tag, [j], []))
+        L = [f"static int xgl_{n}_{gid}_{tag}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s) {{"]
+        L += self.check_levels(sweeps, s)
+        L += self.fill_params(tag, sweeps, s.slot, s)
+        L += [f"  p.m{j} = xg_mask_device(G[{s.slot}].mask);",
+              "  int64_t ntiles = 0;",
+              f"  XG_TRY(xg_mask_tiles(G[{s.slot}].mask, tl, 0, &p.tzero{j}, NULL, NULL, &ntiles));",
+              "  if (ntiles != p.ntz * p.nty * p.ntx) XG_FAIL(\"tile table mismatch\");"]
+        if implicit_scatter:
+            src = self.bname((s.slot, s.level, s.read_version_of_target))
+            dst = self.bname((s.slot, s.level, s.write_version))
+            L.append(f"  XG_CUDA(cudaMemcpyAsync(p.{dst}, p.{src}, (size_t)(p.e{s.slot}[0] * p.e{s.slot}[1] * "
+                     f"p.e{s.slot}[2]) * sizeof(*p.{dst}), cudaMemcpyDeviceToDevice, s));")
+        L += ["  dim3 block(tl[3], tl[4], tl[5]);",
+              f"  xgk_{n}_{gid}_{tag}<<<(unsigned)ntiles, block, 0, s>>>(p);",
+              "  XG_CUDA(cudaGetLastError());"]
+        if s.implicit:
+            L.append(f"  {{ void* t_ = G[{s.slot}].level[{s.level}]; G[{s.slot}].level[{s.level}] = "
+                     f"G[{s.slot}].scratch; G[{s.slot}].scratch = t_; }}")
+        L += ["  return 0;", "}"]
+        self.gen.host_chunks.append("\n".join(L))
+
+    def emit_bnd_single(self, j: int, s) -> None:
+        n, gid = self.name, self.gid
+        tag = f"s{j}"
+        sweeps = [s]
+        extra = ["const int64_t* cells", "int64_t ncells"]
+        self.gen.device_chunks.append(self.params_struct(tag, sweeps, extra))
+        dst = self.bname((s.slot, s.level, s.write_version))
+        pre, val = self.value_code(s, False, "    ")
+        K = [f"__global__ void __launch_bounds__(256) xgk_{n}_{gid}_{tag}(const __grid_constant__ "
+             f"struct xgp_{n}_{gid}_{tag} p) {{",
+             "  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < p.ncells; "
+             "e += (int64_t)gridDim.x * blockDim.x) {",
+             "    const int64_t c = p.cells[e];",
+             f"    const int64_t x = c % p.e{s.slot}[2], y = (c / p.e{s.slot}[2]) % p.e{s.slot}[1], "
+             f"z = c / (p.e{s.slot}[2] * p.e{s.slot}[1]);",
+             "    (void)x; (void)y; (void)z;"]
+        K += pre
+        if any(s.store_offset):
+            oz, oy, ox = s.store_offset
+            e = f"p.e{s.slot}"
+            K.append(f"    xg_stc(p.{dst}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, {e}[0], {e}[1], {e}[2]), "
+                     f"({self.elem(s.slot)})({val}));")
+        else:
+            K.append(f"    p.{dst}[c] = {val};")
+        K += ["  }", "}"]
+        self.gen.device_chunks.append("\n".join(K))
+        L = [f"static int xgl_{n}_{gid}_{tag}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s) {{"]
+        L += self.check_levels(sweeps, s)
+        L += self.fill_params(tag, sweeps, s.slot, s)
+        L += [f"  XG_TRY(xg_mask_cells(G[{s.slot}].mask, {s.mask}, &p.cells, &p.ncells));",
+              "  if (p.ncells == 0) return 0;",
+              "  int64_t nb = (p.ncells + 255) / 256; if (nb > 65535) nb = 65535;",
+              f"  xgk_{n}_{gid}_{tag}<<<(unsigned)nb, 256, 0, s>>>(p);",
+              "  XG_CUDA(cudaGetLastError());",
+              "  return 0;", "}"]
+        self.gen.host_chunks.append("\n".join(L))
+
+    def emit_fused(self) -> None:
+        n, gid = self.name, self.gid
+        tag = "fused"
+        sweeps = self.g.sweeps
+        mains = [j for j, s in enumerate(sweeps) if s.is_main]
+        bnds = [j for j, s in enumerate(sweeps) if not s.is_main]
+        extra = []
+        for j in mains:
+            extra += [f"const int32_t* m{j}", f"const uint8_t* tzero{j}"]
+        for j in bnds:
+            extra += [f"const int32_t* bo{j}", f"const int64_t* bc{j}"]
+        self.gen.device_chunks.append(self.params_struct(tag, sweeps, extra))
+        self.gen.device_chunks.append(self.main_kernel(tag, mains, bnds))
+        dom = sweeps[mains[0]].slot
+        L = [f"static int xgl_{n}_{gid}_{tag}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s) {{"]
+        L += self.check_levels(sweeps)
+        L += self.fill_params(tag, sweeps, dom)
+        for j in mains + bnds:
+            L.append(f"  if (!xg_same_ext(xg_extent(&G[{sweeps[j].slot}]), dom)) return 0;")
+        L.append("  int64_t ntiles = 0;")
+        for j in mains:
+            sj = sweeps[j]
+            L += [f"  p.m{j} = xg_mask_device(G[{sj.slot}].mask);",
+                  f"  XG_TRY(xg_mask_tiles(G[{sj.slot}].mask, tl, 0, &p.tzero{j}, NULL, NULL, &ntiles));"]
+        for j in bnds:
+            sj = sweeps[j]
+            L.append(f"  XG_TRY(xg_mask_tiles(G[{sj.slot}].mask, tl, {sj.mask}, NULL, &p.bo{j}, &p.bc{j}, &ntiles));")
+        for j, offs in self.g.local_checks:
+            sj = sweeps[j]
+            flat = ", ".join(str(v) for o in offs for v in o)
+            L += ["  {", f"    static const int32_t offs[] = {{{flat}}};", "    int ok = 0;",
+                  f"    XG_TRY(xg_mask_tile_local(G[{sj.slot}].mask, tl, {sj.mask}, {len(offs)}, offs, "
+                  f"xg_overstep, &ok));",
+                  "    if (!ok) return 0;", "  }"]
+        L += ["  if (ntiles != p.ntz * p.nty * p.ntx) XG_FAIL(\"tile table mismatch\");",
+              "  dim3 block(tl[3], tl[4], tl[5]);",
+              f"  xgk_{n}_{gid}_{tag}<<<(unsigned)ntiles, block, 0, s>>>(p);",
+              "  XG_CUDA(cudaGetLastError());"]
+        for s in sweeps:
+            if s.implicit:
+                L.append(f"  {{ void* t_ = G[{s.slot}].level[{s.level}]; G[{s.slot}].level[{s.level}] = "
+                         f"G[{s.slot}].scratch; G[{s.slot}].scratch = t_; }}")
+        L += ["  return 1;", "}"]
+        self.gen.host_chunks.append("\n".join(L))
+
+
+def source_digest(source: str, flags: list) -> str:
+    return hashlib.md5(("\n".join(flags) + "\n" + source).encode()).hexdigest()

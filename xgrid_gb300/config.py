@@ -1,0 +1,103 @@
+"""Global configuration set by ``xgrid.init``.
+
+Keyword signature and defaults follow xgrid/util/init.py:48-66 (``parallel``, ``cc``,
+``cacheroot``, ``comment``, ``overstep``, ``opt_level``, ``precision``).  The GPU
+backend keeps their meaning where one exists:
+
+* ``precision`` decides the width of ``float`` at parse time (4 or 8 bytes), as in
+  the reference (xgrid/util/init.py:34-36, xgrid/util/typing/annotation.py:41-42).
+* ``overstep`` selects neighbour addressing at the domain edge: ``none`` (row-major
+  flattened offset, reads outside the allocation return 0), ``limit`` (clamp) or
+  ``wrap`` (periodic).
+* ``opt_level`` maps to ``nvcc -O``; ``cacheroot`` holds the md5-keyed ``.cu``/``.so``.
+* ``parallel`` and ``cc`` are accepted and ignored: every sweep runs on the GPU.
+
+Backend options (new keywords, all optional):
+
+* ``exact``: ``True`` compiles device code with ``--fmad=false`` and host code with
+  ``-ffp-contract=off`` so FP64 results are bit-identical to the reference's C
+  backend; ``False`` lets the compilers contract multiply-adds (results within
+  1e-12 relative of the exact path).
+* ``mixed``: ``None`` (plain), ``"fp32"``, ``"fp16"`` or ``"bf16"``: run the
+  iterations of affine in-place (Jacobi) loops on an FP32/FP16/BF16 defect with
+  FP64 residual and correction passes (see ``xgrid_gb300.mixed``).
+* ``graph``: capture each distinct kernel call into a CUDA graph and replay it.
+* ``fuse``: fuse consecutive sweeps into one launch where the masks allow it.
+* ``divisor``: precompute loop-invariant divisors on the host and divide with a
+  correctly rounded multiply/FMA sequence (checked per divisor).
+"""
+from __future__ import annotations
+
+import dataclasses
+import sys
+from typing import Literal, Optional
+
+from .log import Logger
+
+logger = Logger("xgrid")
+
+_OVERSTEP = ("none", "limit", "wrap")
+_PRECISION = ("float", "double")
+_MIXED = (None, "fp32", "fp16", "bf16")
+
+
+@dataclasses.dataclass
+class Configuration:
+    parallel: bool
+    cc: list
+    cacheroot: str
+    comment: bool
+    overstep: Literal["none", "limit", "wrap"]
+    opt_level: Literal[0, 1, 2, 3]
+    precision: Literal["float", "double"]
+    exact: bool = True
+    mixed: Optional[str] = None
+    graph: bool = True
+    fuse: bool = True
+    divisor: bool = True
+    mixed_every: int = 0
+
+    def __repr__(self) -> str:
+        return repr(dataclasses.asdict(self))
+
+    @property
+    def fsize(self) -> int:
+        return 4 if self.precision == "float" else 8
+
+    @property
+    def nvcc_flags(self) -> list[str]:
+        flags = [f"-O{self.opt_level}"]
+        if self.exact:
+            flags += ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]
+        return flags
+
+
+_config: Configuration | None = None
+
+
+def get_config() -> Configuration:
+    if _config is None:
+        logger.dead("Please call init first to initialize")
+    return _config
+
+
+def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str = ".xgrid",
+         comment: bool = False, overstep: Literal["none", "limit", "wrap"] = "none",
+         opt_level: Literal[0, 1, 2, 3] = 2, precision: Literal["float", "double"] = "float",
+         exact: bool = True, mixed: Optional[str] = None, graph: bool = True,
+         fuse: bool = True, divisor: bool = True, mixed_every: int = 0) -> None:
+    """Set the global configuration (same keywords as the reference plus GPU options)."""
+    global _config
+    if sys.version_info < (3, 10):
+        logger.fail(f"Minimum Python 3.10 is required, current version is {sys.version_info}")
+    if overstep not in _OVERSTEP:
+        logger.dead(f"Invalid overstep '{overstep}', expected one of {_OVERSTEP}")
+    if precision not in _PRECISION:
+        logger.dead(f"Invalid precision '{precision}', expected one of {_PRECISION}")
+    if mixed not in _MIXED:
+        logger.dead(f"Invalid mixed precision '{mixed}', expected one of {_MIXED}")
+    if opt_level not in (0, 1, 2, 3):
+        logger.dead(f"Invalid opt_level '{opt_level}'")
+    _config = Configuration(parallel, list(cc), cacheroot, comment, overstep, opt_level,
+                            precision, exact, mixed, graph, fuse, divisor, int(mixed_every))
+    logger.info(f"initialized with configuration: {_config}")

@@ -1,0 +1,403 @@
+// Runtime of the GB300 stencil backend: error channel, boundary-mask index
+// tables and the CUDA-graph call cache.  C ABI declared in include/xgrid_gb300.h.
+//
+// The reference filters every sweep cell by `boundary_mask[id] == k`
+// (xgrid/lang/generator.py:295-298), so a boundary sweep scans the whole grid to
+// update O(N) cells.  Here the mask is precompiled once per upload into
+//   * per-value cell lists (a boundary sweep launches over its list only), and
+//   * per-tiling tables: a "tile has only mask-0 cells" flag (the interior
+//     sweep skips the mask read there) and the cells of each nonzero value
+//     grouped by tile (a fused launch processes its own tile's boundary cells).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <list>
+#include <map>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "xgrid_gb300.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(const std::string& msg) {
+  g_error = msg;
+  return -1;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+#define XG_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+template <typename T>
+int upload(const std::vector<T>& host, T** dev) {
+  *dev = nullptr;
+  size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(T);
+  XG_CUDA(cudaMalloc(reinterpret_cast<void**>(dev), bytes));
+  if (!host.empty()) XG_CUDA(cudaMemcpy(*dev, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+struct TileKey {
+  int32_t tz, ty, tx;
+  bool operator<(const TileKey& o) const {
+    return std::tie(tz, ty, tx) < std::tie(o.tz, o.ty, o.tx);
+  }
+};
+
+struct Csr {
+  int32_t* off = nullptr;
+  int64_t* cells = nullptr;
+};
+
+struct Tiles {
+  int64_t ntiles = 0;
+  int32_t nt[3] = {1, 1, 1};
+  uint8_t* zero = nullptr;
+  std::map<int32_t, Csr> csr;
+};
+
+}  // namespace
+
+struct xg_mask {
+  int ndim = 0;
+  int64_t ext[3] = {1, 1, 1};  // collapsed z, y, x extents
+  int64_t total = 0;
+  uint64_t version = 0;
+  std::vector<int32_t> host;
+  int32_t* dev = nullptr;
+  std::map<int32_t, std::vector<int64_t>> cells;      // nonzero value -> sorted cells
+  std::map<int32_t, int64_t*> cells_dev;
+  std::map<TileKey, Tiles> tiles;
+  std::map<std::string, int> local_cache;
+
+  void release_tables() {
+    for (auto& kv : cells_dev) cudaFree(kv.second);
+    cells_dev.clear();
+    for (auto& kv : tiles) {
+      cudaFree(kv.second.zero);
+      for (auto& c : kv.second.csr) {
+        cudaFree(c.second.off);
+        cudaFree(c.second.cells);
+      }
+    }
+    tiles.clear();
+    local_cache.clear();
+  }
+};
+
+namespace {
+
+inline int64_t tile_count(int64_t n, int32_t t) { return std::max<int64_t>(1, n / t); }
+inline int64_t tile_of(int64_t c, int32_t t, int64_t nt) { return std::min<int64_t>(c / t, nt - 1); }
+
+int64_t tile_id(const xg_mask* m, const Tiles& T, const TileKey& k, int64_t lin) {
+  int64_t x = lin % m->ext[2];
+  int64_t y = (lin / m->ext[2]) % m->ext[1];
+  int64_t z = lin / (m->ext[2] * m->ext[1]);
+  int64_t iz = tile_of(z, k.tz, T.nt[0]), iy = tile_of(y, k.ty, T.nt[1]), ix = tile_of(x, k.tx, T.nt[2]);
+  return (iz * T.nt[1] + iy) * T.nt[2] + ix;
+}
+
+// Linear index addressed from (z,y,x)+(oz,oy,ox) under an overstep mode, or -1
+// when the access falls outside the allocation in mode "none".
+int64_t address(const xg_mask* m, int64_t lin, const int32_t* o, int overstep) {
+  int64_t X = m->ext[2], Y = m->ext[1], Z = m->ext[0];
+  int64_t x = lin % X, y = (lin / X) % Y, z = lin / (X * Y);
+  if (overstep == XG_OVERSTEP_NONE) {
+    int64_t t = lin + (int64_t)o[0] * X * Y + (int64_t)o[1] * X + o[2];
+    return (t < 0 || t >= m->total) ? -1 : t;
+  }
+  int64_t c[3] = {z + o[0], y + o[1], x + o[2]}, n[3] = {Z, Y, X};
+  for (int d = 0; d < 3; ++d) {
+    if (overstep == XG_OVERSTEP_WRAP) {
+      c[d] = ((c[d] % n[d]) + n[d]) % n[d];
+    } else {
+      c[d] = std::min<int64_t>(std::max<int64_t>(c[d], 0), n[d] - 1);
+    }
+  }
+  return (c[0] * Y + c[1]) * X + c[2];
+}
+
+// ---------------------------------------------------------------- graph cache
+struct GraphEntry {
+  std::vector<uint8_t> key;
+  bool captured = false;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<std::array<void*, XG_MAX_LEVELS + 1>> post;  // level[] + scratch per grid
+  std::vector<uint8_t> ret;
+};
+
+std::mutex g_graph_mu;
+std::list<GraphEntry> g_graphs;  // most recently used first
+constexpr size_t kMaxGraphs = 32;
+
+std::vector<uint8_t> make_key(xg_entry_fn fn, const xg_grid* g, int n, const void* args, size_t nargs) {
+  std::vector<uint8_t> k;
+  auto put = [&k](const void* p, size_t b) {
+    const uint8_t* c = static_cast<const uint8_t*>(p);
+    k.insert(k.end(), c, c + b);
+  };
+  put(&fn, sizeof(fn));
+  put(&n, sizeof(n));
+  put(&nargs, sizeof(nargs));
+  if (nargs) put(args, nargs);
+  for (int i = 0; i < n; ++i) {
+    put(&g[i].ndim, sizeof(int32_t));
+    put(&g[i].levels, sizeof(int32_t));
+    put(g[i].shape, sizeof(g[i].shape));
+    put(g[i].level, sizeof(g[i].level));
+    put(&g[i].scratch, sizeof(void*));
+    put(&g[i].mask, sizeof(void*));
+    uint64_t v = g[i].mask ? g[i].mask->version : 0;
+    put(&v, sizeof(v));
+  }
+  return k;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* xg_last_error(void) { return g_error.c_str(); }
+
+void xg_set_error(const char* message) { g_error = message ? message : ""; }
+
+int xg_runtime_version(void) { return 1; }
+
+int xg_mask_create(int ndim, const int64_t* shape, xg_mask** out) {
+  if (!out) return fail("xg_mask_create: null output");
+  if (ndim < 1 || ndim > XG_MAX_DIM) return fail("xg_mask_create: grids must have 1 to 3 dimensions");
+  xg_mask* m = new xg_mask();
+  m->ndim = ndim;
+  int64_t e[3] = {1, 1, 1};
+  for (int d = 0; d < ndim; ++d) {
+    if (shape[d] <= 0) {
+      delete m;
+      return fail("xg_mask_create: every extent must be positive");
+    }
+    e[3 - ndim + d] = shape[d];
+  }
+  std::memcpy(m->ext, e, sizeof(e));
+  m->total = e[0] * e[1] * e[2];
+  *out = m;
+  return 0;
+}
+
+int xg_mask_destroy(xg_mask* m) {
+  if (!m) return 0;
+  m->release_tables();
+  cudaFree(m->dev);
+  delete m;
+  return 0;
+}
+
+int xg_mask_upload(xg_mask* m, const int32_t* host) {
+  if (!m || !host) return fail("xg_mask_upload: null argument");
+  m->release_tables();
+  m->host.assign(host, host + m->total);
+  m->cells.clear();
+  for (int64_t i = 0; i < m->total; ++i)
+    if (m->host[i] != 0) m->cells[m->host[i]].push_back(i);
+  if (!m->dev) XG_CUDA(cudaMalloc(reinterpret_cast<void**>(&m->dev), m->total * sizeof(int32_t)));
+  XG_CUDA(cudaMemcpy(m->dev, m->host.data(), m->total * sizeof(int32_t), cudaMemcpyHostToDevice));
+  m->version += 1;
+  return 0;
+}
+
+uint64_t xg_mask_version(const xg_mask* m) { return m ? m->version : 0; }
+
+const int32_t* xg_mask_device(const xg_mask* m) { return m ? m->dev : nullptr; }
+
+int xg_mask_cells(xg_mask* m, int32_t value, const int64_t** cells, int64_t* count) {
+  if (!m || !cells || !count) return fail("xg_mask_cells: null argument");
+  if (value == 0) return fail("xg_mask_cells: mask value 0 has no cell list");
+  auto it = m->cells.find(value);
+  if (it == m->cells.end()) {
+    *cells = nullptr;
+    *count = 0;
+    return 0;
+  }
+  auto d = m->cells_dev.find(value);
+  if (d == m->cells_dev.end()) {
+    int64_t* p = nullptr;
+    if (upload(it->second, &p)) return -1;
+    d = m->cells_dev.emplace(value, p).first;
+  }
+  *cells = d->second;
+  *count = static_cast<int64_t>(it->second.size());
+  return 0;
+}
+
+int xg_mask_tiles(xg_mask* m, const int32_t* tile, int32_t value, const uint8_t** tile_zero,
+                  const int32_t** csr_off, const int64_t** csr_cells, int64_t* ntiles) {
+  if (!m || !tile) return fail("xg_mask_tiles: null argument");
+  if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1) return fail("xg_mask_tiles: tile extents must be positive");
+  TileKey key{tile[0], tile[1], tile[2]};
+  auto it = m->tiles.find(key);
+  if (it == m->tiles.end()) {
+    Tiles T;
+    T.nt[0] = (int32_t)tile_count(m->ext[0], key.tz);
+    T.nt[1] = (int32_t)tile_count(m->ext[1], key.ty);
+    T.nt[2] = (int32_t)tile_count(m->ext[2], key.tx);
+    T.ntiles = (int64_t)T.nt[0] * T.nt[1] * T.nt[2];
+    if (T.ntiles > INT32_MAX) return fail("xg_mask_tiles: too many tiles");
+    std::vector<uint8_t> zero(T.ntiles, 1);
+    for (auto& kv : m->cells)
+      for (int64_t c : kv.second) zero[tile_id(m, T, key, c)] = 0;
+    if (upload(zero, &T.zero)) return -1;
+    it = m->tiles.emplace(key, T).first;
+  }
+  Tiles& T = it->second;
+  if (tile_zero) *tile_zero = T.zero;
+  if (ntiles) *ntiles = T.ntiles;
+  if (value != 0 && (csr_off || csr_cells)) {
+    auto c = T.csr.find(value);
+    if (c == T.csr.end()) {
+      std::vector<int32_t> off(T.ntiles + 1, 0);
+      std::vector<int64_t> sorted;
+      auto cv = m->cells.find(value);
+      if (cv != m->cells.end()) {
+        std::vector<std::pair<int64_t, int64_t>> tagged;
+        tagged.reserve(cv->second.size());
+        for (int64_t cell : cv->second) tagged.emplace_back(tile_id(m, T, key, cell), cell);
+        std::sort(tagged.begin(), tagged.end());
+        for (auto& p : tagged) {
+          off[p.first + 1] += 1;
+          sorted.push_back(p.second);
+        }
+        for (int64_t t = 0; t < T.ntiles; ++t) off[t + 1] += off[t];
+      }
+      Csr csr;
+      if (upload(off, &csr.off) || upload(sorted, &csr.cells)) return -1;
+      c = T.csr.emplace(value, csr).first;
+    }
+    if (csr_off) *csr_off = c->second.off;
+    if (csr_cells) *csr_cells = c->second.cells;
+  }
+  return 0;
+}
+
+int xg_mask_tile_local(xg_mask* m, const int32_t* tile, int32_t value, int noff, const int32_t* offsets,
+                       int overstep, int* ok) {
+  if (!m || !tile || !ok || (noff > 0 && !offsets)) return fail("xg_mask_tile_local: null argument");
+  std::string ck(reinterpret_cast<const char*>(tile), 3 * sizeof(int32_t));
+  ck.append(reinterpret_cast<const char*>(&value), sizeof(value));
+  ck.append(reinterpret_cast<const char*>(&overstep), sizeof(overstep));
+  ck.append(reinterpret_cast<const char*>(offsets), (size_t)noff * 3 * sizeof(int32_t));
+  auto hit = m->local_cache.find(ck);
+  if (hit != m->local_cache.end()) {
+    *ok = hit->second;
+    return 0;
+  }
+  if (xg_mask_tiles(m, tile, 0, nullptr, nullptr, nullptr, nullptr)) return -1;
+  TileKey key{tile[0], tile[1], tile[2]};
+  const Tiles& T = m->tiles.at(key);
+  int result = 1;
+  auto cv = m->cells.find(value);
+  if (cv != m->cells.end()) {
+    for (int64_t c : cv->second) {
+      int64_t own = tile_id(m, T, key, c);
+      for (int k = 0; k < noff && result; ++k) {
+        int64_t t = address(m, c, offsets + 3 * k, overstep);
+        if (t >= 0 && tile_id(m, T, key, t) != own) result = 0;
+      }
+      if (!result) break;
+    }
+  }
+  m->local_cache.emplace(ck, result);
+  *ok = result;
+  return 0;
+}
+
+int xg_call(xg_entry_fn fn, xg_grid* grids, int ngrids, const void* args, size_t nargs, void* ret, size_t nret,
+            void* stream, int use_graph) {
+  if (!fn) return fail("xg_call: null entry point");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!use_graph || s == nullptr) return fn(grids, ngrids, args, nargs, ret, nret, stream);
+
+  std::vector<uint8_t> key = make_key(fn, grids, ngrids, args, nargs);
+  std::unique_lock<std::mutex> lock(g_graph_mu);
+  auto it = std::find_if(g_graphs.begin(), g_graphs.end(), [&](const GraphEntry& e) { return e.key == key; });
+  if (it == g_graphs.end()) {
+    // first sighting: run eagerly (this builds any mask tables the body needs)
+    GraphEntry e;
+    e.key = key;
+    g_graphs.push_front(std::move(e));
+    while (g_graphs.size() > kMaxGraphs) {
+      if (g_graphs.back().exec) cudaGraphExecDestroy(g_graphs.back().exec);
+      g_graphs.pop_back();
+    }
+    lock.unlock();
+    return fn(grids, ngrids, args, nargs, ret, nret, stream);
+  }
+  g_graphs.splice(g_graphs.begin(), g_graphs, it);
+  GraphEntry& e = g_graphs.front();
+  if (!e.captured) {
+    XG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = fn(grids, ngrids, args, nargs, ret, nret, stream);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (rc != 0) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    cudaError_t ie = cudaGraphInstantiate(&e.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
+    e.captured = true;
+    e.post.resize(ngrids);
+    for (int i = 0; i < ngrids; ++i) {
+      std::copy(grids[i].level, grids[i].level + XG_MAX_LEVELS, e.post[i].begin());
+      e.post[i][XG_MAX_LEVELS] = grids[i].scratch;
+    }
+    e.ret.assign(static_cast<uint8_t*>(ret), static_cast<uint8_t*>(ret) + (ret ? nret : 0));
+  } else {
+    for (int i = 0; i < ngrids; ++i) {
+      std::copy(e.post[i].begin(), e.post[i].begin() + XG_MAX_LEVELS, grids[i].level);
+      grids[i].scratch = e.post[i][XG_MAX_LEVELS];
+    }
+    if (ret && nret) std::memcpy(ret, e.ret.data(), std::min(nret, e.ret.size()));
+  }
+  XG_CUDA(cudaGraphLaunch(e.exec, s));
+  return 0;
+}
+
+int xg_graph_clear(xg_entry_fn fn) {
+  std::lock_guard<std::mutex> lock(g_graph_mu);
+  for (auto it = g_graphs.begin(); it != g_graphs.end();) {
+    xg_entry_fn owner;
+    std::memcpy(&owner, it->key.data(), sizeof(owner));
+    if (fn == nullptr || owner == fn) {
+      if (it->exec) cudaGraphExecDestroy(it->exec);
+      it = g_graphs.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  return 0;
+}
+
+int64_t xg_graph_count(void) {
+  std::lock_guard<std::mutex> lock(g_graph_mu);
+  int64_t n = 0;
+  for (auto& e : g_graphs) n += e.captured ? 1 : 0;
+  return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+"""``@xgrid.kernel`` / ``@xgrid.function`` / ``@xgrid.external`` operators.
+
+Call protocol of xgrid/lang/operator.py:13-64: a kernel parses and compiles on
+its first call, then on every call ticks each ``Grid`` argument to the kernel's
+time depth (in argument order) and invokes the native entry point.  Here the
+native entry point is the generated CUDA module, called through the runtime's
+graph cache (``xg_call``) on the backend stream; the call is asynchronous except
+for kernels that return a value.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Any, Callable
+
+from . import ir
+from .log import Logger
+from .types import BaseType, Void
+
+CustomTypecheck = Callable[[list], BaseType]
+
+
+class Operator:
+    def __init__(self, func, mode: str, name: str | None = None, includes: list | None = None,
+                 self_type: BaseType | None = None, typecheck_override: CustomTypecheck | None = None,
+                 tick: bool = True, macro: list | None = None) -> None:
+        self.func = func
+        self.mode = mode
+        self.logger = Logger(self)
+        self.name = func.__name__ if name is None else name
+        self.includes = [] if includes is None else list(includes)
+        self.macro = [] if macro is None else list(macro)
+        self.native = None
+        self.self_type = self_type
+        self.typecheck_override = typecheck_override
+        self.tick = tick
+
+    def __call__(self, *args: Any) -> Any:
+        if self.mode == "kernel":
+            if self.native is None:
+                from .native import NativeKernel
+                self.native = NativeKernel(self)
+            return self.native(*args)
+        if self.mode == "function":
+            return self.func(*args)
+        self.logger.dead(f"Invalid call to non-kernel or non-function ({self.mode}) operator '{self.name}'")
+
+    @property
+    def ir(self) -> ir.Definition:
+        cached = getattr(self, "_ir", None)
+        if cached is None:
+            from .parser import Parser
+            parser = Parser(self.func, self.name, self.mode, self.self_type)
+            self._ir = cached = parser.result
+            self.includes.extend(i for i in parser.includes if i not in self.includes)
+        return cached
+
+    @property
+    def src(self) -> str:
+        """Generated CUDA source of this kernel."""
+        from .codegen import CudaGenerator
+        from .config import get_config
+        return CudaGenerator(self, get_config()).generate().source
+
+    @property
+    def signature(self) -> ir.Signature:
+        return self.ir.signature
+
+
+def kernel(*, name: str | None = None, includes: list | None = None, tick: bool = True,
+           macro: list | None = None):
+    def aux(func):
+        return Operator(func, "kernel", name, includes, tick=tick, macro=macro)
+    return aux
+
+
+def function(*, method: bool = False, name: str | None = None, includes: list | None = None,
+             macro: list | None = None):
+    if method:
+        def aux_method(func):
+            setattr(func, "__xgrid_method", (name, includes))
+            return func
+        return aux_method
+
+    def aux(func):
+        return Operator(func, "function", name, includes, macro=macro)
+    return aux
+
+
+def external(*, name: str | None = None, includes: list | None = None, typecheck_override: CustomTypecheck):
+    def aux(func):
+        return Operator(func, "external", name, includes, typecheck_override=typecheck_override)
+    return aux
