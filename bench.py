@@ -1,0 +1,360 @@
+#!/usr/bin/env python
+"""Benchmark of the stencil hot path on one GB300 (or N replicas).
+
+Workload (default): the lid-driven cavity program on 1025 x 1025 FP64 grids,
+dt = 1e-5, zero initial fields; one *step* is one call of the cavity kernel
+(1 source sweep, 1 + 50 Jacobi sweeps of the pressure with four boundary passes
+each, 2 momentum sweeps, velocity walls).  Metric: GLUP/s, counting one lattice
+update per cell per full-grid sweep (54 per step; boundary passes excluded).
+
+* ``value``: device time of K steps (CUDA events on the backend stream around
+  each step, L2 flushed between steps by writing a 256 MiB buffer), grids
+  resident in HBM.
+* ``e2e``: the same steps through the public API with host buffers: every step
+  reads ``u.now``, ``v.now``, ``p.now`` back (device→host) and the next call
+  uploads them again (host→device, pinned), wall clock around the loop.
+* ``roofline``: the dominant kernel (the fused Jacobi + boundary launch), its
+  algorithmic bytes per launch over its mean duration from CUDA events recorded
+  around every launch during a profiled (non-graph) pass of the same steps.
+* ``cpu_baseline``: the reference's own generated C (compiled from
+  ``oracle/_ref``) on all host cores for a bounded number of steps.
+
+``--impl reference`` times that reference C path alone on the host cores.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SWEEPS_PER_STEP = 54  # b, 1 + 50 Jacobi, u, v
+METRIC = "GLUP/s & HBM-roofline % per stencil: mixed/batched vs plain FP64, same GB300"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1025)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help=argparse.SUPPRESS)
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_tag: str):
+    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int) -> None:
+        self.index = index
+        self.proc = None
+        self.path = tempfile.mktemp(prefix="xgclk", suffix=".csv")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_sample(n: int, steps: int) -> dict:
+    """Run the reference C (or the C restatement) for ``steps`` steps; seconds."""
+    from oracle import native
+    kind = "reference" if (native.ref_available() or os.path.isdir(native.REF)) else "port"
+    try:
+        o = native.Oracle(kind, exact=False)
+    except Exception:  # noqa: BLE001 - the reference sources are absent
+        kind = "port"
+        o = native.Oracle("port")
+    f = native.cavity_fields(n)
+    cfg = (1.0, 0.1, 1e-5, 2.0 / (n - 1), 2.0 / (n - 1))
+    o.cavity(f, cfg, 1)  # warm-up (page faults, thread team)
+    t0 = time.perf_counter()
+    o.cavity(f, cfg, steps)
+    dt = time.perf_counter() - t0
+    return {"kind": kind, "seconds": dt, "steps": steps}
+
+
+def run_cpu(n: int, steps: int) -> dict:
+    cores = os.cpu_count() or 1
+    env = dict(os.environ, OMP_NUM_THREADS=str(cores), OMP_PROC_BIND="close")
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-sample", str(steps), "--n", str(n)]
+    out = subprocess.run(cmd, env=env, capture_output=True, text=True, check=True).stdout.strip().splitlines()[-1]
+    r = json.loads(out)
+    r["cores"] = cores
+    return r
+
+
+def cpu_baseline(n: int, seconds: float) -> dict:
+    probe = run_cpu(n, 1)
+    steps = max(2, min(400, int(math.ceil(seconds / max(probe["seconds"], 1e-3)))))
+    r = run_cpu(n, steps)
+    lups = SWEEPS_PER_STEP * n * n * r["steps"]
+    return {"value": lups / r["seconds"] / 1e9, "unit": "GLUP/s", "cores": r["cores"], "kind": r["kind"],
+            "sample": f"cavity {n}x{n} FP64, {r['steps']} steps ({r['seconds']:.1f} s), OpenMP on all host cores"}
+
+
+# ---------------------------------------------------------------- GPU side
+def gpu_bench(args, rank: int, world: int):
+    import torch
+
+    import xgrid
+    import workloads
+    from xgrid_gb300 import device, runtime
+
+    torch.cuda.set_device(rank % max(torch.cuda.device_count(), 1))
+    cache = os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}")
+    xgrid.init(precision="double", cacheroot=cache, opt_level=3)
+    n = args.n
+    grids, cfg = workloads.cavity_setup(n, 1e-5)
+    kern = workloads.cavity_kernel
+    b, p, u, v = grids["b"], grids["p"], grids["u"], grids["v"]
+
+    def step():
+        kern(b, p, u, v, cfg)
+
+    for _ in range(args.warmup):
+        step()
+    s = device.stream()
+    s.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    lib = runtime.load()
+
+    def timed(k: int):
+        evs = []
+        for _ in range(k):
+            with torch.cuda.stream(s):
+                flush.add_(1)  # L2 flush: 256 MiB read+write, outside the timed interval
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            step()
+            e1.record(s)
+            evs.append((e0, e1))
+        s.synchronize()
+        return sum(a.elapsed_time(b_) for a, b_ in evs) / 1000.0
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        secs = timed(args.steps)
+    torch.cuda.synchronize()
+    if world > 1:
+        t = torch.tensor([secs], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        secs = float(t.item())
+        torch.distributed.barrier()
+    lups_rank = SWEEPS_PER_STEP * n * n * args.steps
+
+    # profiled pass (eager, CUDA events around every launch)
+    native_k = kern.native
+    native_k.use_graph = False
+    lib.xg_prof_reset()
+    lib.xg_prof_enable(1)
+    prof_steps = min(args.steps, 10)
+    for _ in range(prof_steps):
+        step()
+    s.synchronize()
+    lib.xg_prof_enable(0)
+    recs = runtime.prof_records()
+    launches_per_step = len(recs) / prof_steps
+    lib.xg_prof_reset()
+    native_k.use_graph = True
+    by_site = {}
+    for g, ms in recs:
+        by_site.setdefault(g, []).append(ms)
+    dom_site, dom_ms = max(by_site.items(), key=lambda kv: sum(kv[1]))
+    dom_avg_s = statistics.mean(dom_ms) / 1000.0
+    total_prof = sum(sum(x) for x in by_site.values())
+    group = dom_site // 64
+    bytes_per_cell = algorithmic_bytes(native_k.module, group)
+    alg_bytes = bytes_per_cell * n * n
+    hbm_peak, peak_src = peaks()
+    achieved = alg_bytes / dom_avg_s / 1e9
+    tag = "cavity_jacobi_fused_fp64"
+    traffic = profile_traffic(tag)
+    if traffic is not None:
+        traffic = traffic * (n * n) / (1025 * 1025)
+
+    # e2e through the public API with host buffers
+    for g in (u, v, p):
+        g.now  # noqa: B018 - host copies become current and authoritative
+    torch.cuda.synchronize()
+    e2e_steps = args.e2e_steps
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        step()
+        for g in (u, v, p):
+            g.now  # noqa: B018 - device→host read of the step's result
+    s.synchronize()
+    e2e_secs = time.perf_counter() - t0
+    level_bytes = n * n * 8
+    e2e = {"value": SWEEPS_PER_STEP * n * n * e2e_steps / e2e_secs / 1e9 * world, "unit": "GLUP/s",
+           "h2d_bytes_per_step": 3 * level_bytes, "d2h_bytes_per_step": 3 * level_bytes,
+           "steps": e2e_steps, "ms_per_step": e2e_secs / e2e_steps * 1e3}
+
+    result = {
+        "metric": METRIC,
+        "value": lups_rank * world / secs / 1e9,
+        "unit": "GLUP/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": secs / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: zero initial fields, lid u=1 (deterministic)",
+        "config": {"workload": f"lid-driven cavity {n}x{n} FP64 plain, dt=1e-5, 50+1 Jacobi sweeps/step, "
+                               f"bit-exact vs reference C",
+                   "n": n, "sweeps_per_step": SWEEPS_PER_STEP, "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": f"replicas x{world}", "graph": True, "launches_per_step": launches_per_step},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                     "kernel": f"group {group} (site {dom_site})", "kernel_ms": dom_avg_s * 1e3,
+                     "kernel_share": sum(dom_ms) / total_prof, "algorithmic_bytes_per_launch": alg_bytes},
+        "e2e": e2e,
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "clocks": clk.summary(),
+    }
+    return result
+
+
+def algorithmic_bytes(module, group: int) -> float:
+    """Bytes per cell of one launch of ``group``: distinct buffers read (not
+    produced earlier in the launch) plus distinct buffers written, main sweeps
+    only (boundary passes touch O(N) cells)."""
+    elem = {i: gt.element.nbytes for i, (_, gt) in enumerate(module.grid_args)}
+    read, written = [], []
+    for s in module.sweeps:
+        if s.group_index != group or not s.is_main:
+            continue
+        for _, ld in s.loads:
+            key = (ld.slot, ld.level, ld.version)
+            if key not in written and key not in read:
+                read.append(key)
+        w = (s.slot, s.level, s.write_version)
+        if w not in written:
+            written.append(w)
+    return float(sum(elem[k[0]] for k in read) + sum(elem[k[0]] for k in written))
+
+
+def reference_arm(args, rank: int, world: int):
+    if rank != 0:
+        return None
+    n = args.n
+    probe = run_cpu(n, 1)
+    per_step = max(1, int(math.ceil(args.cpu_seconds / 10 / max(probe["seconds"], 1e-3))))
+    per_step = min(per_step, 5)
+    run_cpu(n, max(1, args.warmup))
+    r = run_cpu(n, args.steps * per_step if args.steps * per_step * probe["seconds"] < 240 else
+                max(1, int(240 / max(probe["seconds"], 1e-3))))
+    lups = SWEEPS_PER_STEP * n * n * r["steps"]
+    val = lups / r["seconds"] / 1e9
+    return {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "GLUP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["seconds"] / r["steps"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: zero initial fields, lid u=1 (deterministic)",
+        "config": {"workload": f"lid-driven cavity {n}x{n} FP64 plain, dt=1e-5, 50+1 Jacobi sweeps/step", "n": n,
+                   "sweeps_per_step": SWEEPS_PER_STEP},
+        "cpu_baseline": {"value": val, "unit": "GLUP/s", "cores": r["cores"], "kind": r["kind"],
+                         "sample": f"cavity {n}x{n} FP64, {r['steps']} steps ({r['seconds']:.1f} s)"},
+        "e2e": {"value": val, "unit": "GLUP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    if args.cpu_sample:
+        print(json.dumps(cpu_sample(args.n, args.cpu_sample)))
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        out = reference_arm(args, rank, world)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    out = gpu_bench(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

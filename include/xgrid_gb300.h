@@ -115,6 +115,20 @@ int xg_call(xg_entry_fn fn, xg_grid* grids, int ngrids, const void* args, size_t
 int xg_graph_clear(xg_entry_fn fn);
 int64_t xg_graph_count(void);
 
+/* ---- launch accounting (used by generated modules and the benchmark) ----- */
+/* Generated modules call xg_prof_launch() before every kernel launch and
+ * xg_prof_end() after it.  Both only count unless profiling is on; with
+ * profiling on, CUDA events are recorded around each launch on its stream and
+ * xg_prof_read() returns (group id, milliseconds) per launch.  Profiling is for
+ * eager calls only (a captured graph records no events). */
+void xg_prof_enable(int on);
+int xg_prof_enabled(void);
+void xg_prof_launch(int group, void* stream);
+void xg_prof_end(int group, void* stream);
+int64_t xg_prof_launches(void);
+int xg_prof_read(int64_t max, int32_t* groups, float* ms, int64_t* count);
+void xg_prof_reset(void);
+
 #ifdef __cplusplus
 }
 #endif

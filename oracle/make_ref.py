@@ -1,0 +1,48 @@
+"""Write the reference's own generated C for the benchmark programs.
+
+Needs the reference checkout (argv[1], default /root/reference).  For each of
+the two benchmark programs in workloads.py (2-D diffusion, lid-driven cavity)
+it runs the reference's parser and C generator (xgrid/lang/generator.py) and
+writes the C source to oracle/_ref/<kernel>.c.  Those files are not versioned;
+they travel with the working tree and ``oracle.native.build_ref`` compiles them
+with the reference's compiler flags on whatever host runs the baseline.
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+OUT = os.path.join(HERE, "_ref")
+KERNELS = ("diffusion2d", "cavity_kernel")
+
+CHILD = r"""
+import os, sys
+sys.path.insert(0, {ref!r})
+sys.path.insert(1, {root!r})
+import xgrid
+assert os.path.abspath(xgrid.__file__).startswith(os.path.abspath({ref!r}))
+xgrid.init(parallel=True, precision="double", opt_level=3, cacheroot=".xgridref")
+import workloads
+from xgrid.lang.generator import Generator
+for name in {kernels!r}:
+    src = Generator(getattr(workloads, name)).source
+    with open(os.path.join({out!r}, name + ".c"), "w") as f:
+        f.write(src)
+"""
+
+
+def generate(ref: str = "/root/reference") -> list:
+    if not os.path.isdir(os.path.join(ref, "xgrid")):
+        raise FileNotFoundError(f"reference checkout not found at {ref}")
+    os.makedirs(OUT, exist_ok=True)
+    code = CHILD.format(ref=ref, root=ROOT, kernels=KERNELS, out=OUT)
+    with tempfile.TemporaryDirectory() as tmp:
+        subprocess.run([sys.executable, "-c", code], cwd=tmp, check=True)
+    return [os.path.join(OUT, k + ".c") for k in KERNELS]
+
+
+if __name__ == "__main__":
+    for p in generate(*(sys.argv[1:2])):
+        print(p)

@@ -20,7 +20,7 @@ float3d = xgrid.grid[float, 3]
 # ----------------------------------------------------------------- diffusion
 @xgrid.kernel()
 def diffusion2d(u: float2d, c: float) -> None:
-    """Explicit FTCS 5-point heat step, Dirichlet zero on mask 1."""
+    # explicit FTCS 5-point heat step, Dirichlet zero on mask 1
     u[0, 0] = u[0, 0] + c * (u[1, 0] + u[-1, 0] + u[0, 1] + u[0, -1] - 4.0 * u[0, 0])
     with xgrid.boundary(1):
         u[0, 0] = 0.0

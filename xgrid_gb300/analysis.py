@@ -56,6 +56,7 @@ class Sweep:
     loads: list = dataclasses.field(default_factory=list)   # list[(ir.Stencil, Load)]
     write_version: int = 0
     read_version_of_target: int = 0
+    group_index: int = -1
 
     @property
     def is_main(self) -> bool:
@@ -136,6 +137,8 @@ def build_groups(sweeps: list, counter: list, fuse: bool) -> list:
     def close():
         nonlocal current, versions, writes, main_reads
         if current:
+            for member in current:
+                member.group_index = counter[0]
             groups.append(Group(current, counter[0]))
             counter[0] += 1
         current, versions, writes, main_reads = [], {}, set(), set()

@@ -457,8 +457,10 @@ class CudaGenerator:
                f"expected %zu\", nargs, (size_t){'sizeof(a)' if value_args else '0'});",
                "  memset(&a, 0, sizeof a);",
                "  if (nargs) memcpy(&a, args, nargs);",
+               "  xg_prof_launch(-1, s);",
                f"  xgk_{name}_scalar<<<1, 1, 0, s>>>(a);",
-               "  XG_CUDA(cudaGetLastError());"]
+               "  XG_CUDA(cudaGetLastError());",
+               "  xg_prof_end(-1, s);"]
         if not isinstance(rtype, Void):
             out += [f"  if (!ret || nret != sizeof({rt})) XG_FAIL(\"{name}: return buffer has %zu bytes\", nret);",
                     f"  XG_CUDA(cudaMemcpyFromSymbolAsync(ret, xg_ret_{name}, sizeof({rt}), 0, "
@@ -893,9 +895,12 @@ class SweepGroupEmitter:
             dst = self.bname((s.slot, s.level, s.write_version))
             L.append(f"  XG_CUDA(cudaMemcpyAsync(p.{dst}, p.{src}, (size_t)(p.e{s.slot}[0] * p.e{s.slot}[1] * "
                      f"p.e{s.slot}[2]) * sizeof(*p.{dst}), cudaMemcpyDeviceToDevice, s));")
+        site = gid * 64 + j
         L += ["  dim3 block(tl[3], tl[4], tl[5]);",
+              f"  xg_prof_launch({site}, s);",
               f"  xgk_{n}_{gid}_{tag}<<<(unsigned)ntiles, block, 0, s>>>(p);",
-              "  XG_CUDA(cudaGetLastError());"]
+              "  XG_CUDA(cudaGetLastError());",
+              f"  xg_prof_end({site}, s);"]
         if s.implicit:
             L.append(f"  {{ void* t_ = G[{s.slot}].level[{s.level}]; G[{s.slot}].level[{s.level}] = "
                      f"G[{s.slot}].scratch; G[{s.slot}].scratch = t_; }}")
@@ -934,8 +939,10 @@ class SweepGroupEmitter:
         L += [f"  XG_TRY(xg_mask_cells(G[{s.slot}].mask, {s.mask}, &p.cells, &p.ncells));",
               "  if (p.ncells == 0) return 0;",
               "  int64_t nb = (p.ncells + 255) / 256; if (nb > 65535) nb = 65535;",
+              f"  xg_prof_launch({gid * 64 + j}, s);",
               f"  xgk_{n}_{gid}_{tag}<<<(unsigned)nb, 256, 0, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
+              f"  xg_prof_end({gid * 64 + j}, s);",
               "  return 0;", "}"]
         self.gen.host_chunks.append("\n".join(L))
 
@@ -975,8 +982,10 @@ class SweepGroupEmitter:
                   "    if (!ok) return 0;", "  }"]
         L += ["  if (ntiles != p.ntz * p.nty * p.ntx) XG_FAIL(\"tile table mismatch\");",
               "  dim3 block(tl[3], tl[4], tl[5]);",
+              f"  xg_prof_launch({gid * 64 + 63}, s);",
               f"  xgk_{n}_{gid}_{tag}<<<(unsigned)ntiles, block, 0, s>>>(p);",
-              "  XG_CUDA(cudaGetLastError());"]
+              "  XG_CUDA(cudaGetLastError());",
+              f"  xg_prof_end({gid * 64 + 63}, s);"]
         for s in sweeps:
             if s.implicit:
                 L.append(f"  {{ void* t_ = G[{s.slot}].level[{s.level}]; G[{s.slot}].level[{s.level}] = "

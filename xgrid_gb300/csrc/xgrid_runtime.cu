@@ -393,6 +393,80 @@ int xg_graph_clear(xg_entry_fn fn) {
   return 0;
 }
 
+// ------------------------------------------------------------ launch accounting
+namespace {
+struct ProfRec {
+  int32_t group;
+  cudaEvent_t start, stop;
+};
+std::mutex g_prof_mu;
+int g_prof_on = 0;
+int64_t g_launches = 0;
+std::vector<ProfRec> g_prof;
+std::vector<cudaEvent_t> g_event_pool;
+cudaEvent_t pooled_event() {
+  if (!g_event_pool.empty()) {
+    cudaEvent_t e = g_event_pool.back();
+    g_event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+}  // namespace
+
+void xg_prof_enable(int on) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  g_prof_on = on;
+}
+
+int xg_prof_enabled(void) { return g_prof_on; }
+
+void xg_prof_launch(int group, void* stream) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  g_launches += 1;
+  if (!g_prof_on) return;
+  ProfRec r{group, pooled_event(), pooled_event()};
+  cudaEventRecord(r.start, static_cast<cudaStream_t>(stream));
+  g_prof.push_back(r);
+}
+
+void xg_prof_end(int group, void* stream) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  if (!g_prof_on || g_prof.empty() || g_prof.back().group != group) return;
+  cudaEventRecord(g_prof.back().stop, static_cast<cudaStream_t>(stream));
+}
+
+int64_t xg_prof_launches(void) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  return g_launches;
+}
+
+int xg_prof_read(int64_t max, int32_t* groups, float* ms, int64_t* count) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  int64_t n = std::min<int64_t>(max, (int64_t)g_prof.size());
+  for (int64_t i = 0; i < n; ++i) {
+    XG_CUDA(cudaEventSynchronize(g_prof[i].stop));
+    float t = 0.f;
+    XG_CUDA(cudaEventElapsedTime(&t, g_prof[i].start, g_prof[i].stop));
+    if (groups) groups[i] = g_prof[i].group;
+    if (ms) ms[i] = t;
+  }
+  if (count) *count = (int64_t)g_prof.size();
+  return 0;
+}
+
+void xg_prof_reset(void) {
+  std::lock_guard<std::mutex> lock(g_prof_mu);
+  for (auto& r : g_prof) {
+    g_event_pool.push_back(r.start);
+    g_event_pool.push_back(r.stop);
+  }
+  g_prof.clear();
+  g_launches = 0;
+}
+
 int64_t xg_graph_count(void) {
   std::lock_guard<std::mutex> lock(g_graph_mu);
   int64_t n = 0;

@@ -51,7 +51,27 @@ SIGNATURES = {
                                ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int]),
     "xg_graph_clear": (ctypes.c_int, [ctypes.c_void_p]),
     "xg_graph_count": (ctypes.c_int64, []),
+    "xg_prof_enable": (None, [ctypes.c_int]),
+    "xg_prof_enabled": (ctypes.c_int, []),
+    "xg_prof_launch": (None, [ctypes.c_int, ctypes.c_void_p]),
+    "xg_prof_end": (None, [ctypes.c_int, ctypes.c_void_p]),
+    "xg_prof_launches": (ctypes.c_int64, []),
+    "xg_prof_read": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float),
+                                    ctypes.POINTER(ctypes.c_int64)]),
+    "xg_prof_reset": (None, []),
 }
+
+
+def prof_records() -> list:
+    """[(group id, ms)] of the launches recorded while profiling was on."""
+    lib = load()
+    count = ctypes.c_int64()
+    check(lib.xg_prof_read(0, None, None, ctypes.byref(count)), "prof")
+    n = count.value
+    groups = (ctypes.c_int32 * max(n, 1))()
+    ms = (ctypes.c_float * max(n, 1))()
+    check(lib.xg_prof_read(n, groups, ms, ctypes.byref(count)), "prof")
+    return [(groups[i], ms[i]) for i in range(n)]
 
 
 def load(path: str | None = None):
