@@ -72,6 +72,29 @@ typedef struct xg_grid {
 typedef int (*xg_entry_fn)(xg_grid* grids, int ngrids, const void* args, size_t nargs,
                            void* ret, size_t nret, void* stream);
 
+/*
+ * No-alloc variant of an entry point (no counterpart in the reference).
+ * A kernel declared with @xgrid.kernel(noalloc=True) also exports
+ *     xg_kernel_<name>_noalloc
+ * with the signature of xg_entry_fn and the same results as xg_kernel_<name>.
+ * It is meant for callers that cannot call cudaMalloc: code running under a
+ * fixed device-memory budget, inside another framework's allocator, or in a
+ * real-time loop where an allocation may block.  The scratch level that an
+ * in-place (two-phase) sweep needs comes from a static __device__ array of
+ * 64 MiB in the module (held by every GPU that loads the module until the
+ * process exits) instead of grids[i].scratch, which is ignored; calls that
+ * need more than 64 MiB of scratch fail with an error.  The call allocates
+ * nothing: it fails instead if a boundary-mask table it needs has not been
+ * built by an earlier regular call with the same grids.  Its first call on a
+ * device looks up the array's device address (do it before any stream
+ * capture).  All calls share the array, so calls that overlap on the GPU
+ * race; the caller's level pointers are never replaced.
+ */
+typedef xg_entry_fn xg_noalloc_entry_fn;
+#define XG_DECLARE_NOALLOC_ENTRY(name)                                                   \
+    int xg_kernel_##name##_noalloc(xg_grid* grids, int ngrids, const void* args, size_t nargs, \
+                                   void* ret, size_t nret, void* stream)
+
 /* ---- errors -------------------------------------------------------------- */
 const char* xg_last_error(void);
 void xg_set_error(const char* message);

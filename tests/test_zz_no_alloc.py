@@ -1,0 +1,103 @@
+"""No-alloc entry point vs the regular entry point (GPU, through the C ABI).
+
+Some callers cannot call cudaMalloc: code under a fixed device-memory budget,
+code that runs inside another framework's allocator, or a real-time loop where
+an allocation may block.  For them a kernel declared with
+``@xgrid.kernel(noalloc=True)`` exports ``xg_kernel_<name>_noalloc``, which takes
+the scratch level of its in-place (two-phase) sweeps from a 64 MiB pool inside
+the module instead of from the caller.  This file runs last so that a failure
+here does not hide the other tests' results.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import xgrid
+from xgrid_gb300 import device, runtime
+
+pytestmark = pytest.mark.gpu
+
+
+@xgrid.kernel(noalloc=True)
+def relax(p: xgrid.grid[float, 2], f: xgrid.grid[float, 2], iters: int, h2: float) -> None:
+    for _ in range(0, iters):
+        p[0, 0] = 0.25 * (p[1, 0][0] + p[-1, 0][0] + p[0, 1][0] + p[0, -1][0] - h2 * f[0, 0][0])
+        with xgrid.boundary(1):
+            p[0, 0] = p[0, 1][0]
+        with xgrid.boundary(2):
+            p[0, 0] = 0.5
+
+
+def _grids(n: int, seed: int):
+    rng = np.random.default_rng(seed)
+    p = xgrid.Grid((n, n), float)
+    f = xgrid.Grid((n, n), float)
+    p.now[...] = rng.random((n, n))
+    f.now[...] = rng.random((n, n)) - 0.5
+    b = p.boundary
+    b[:, 0] = 1
+    b[0, :] = b[-1, :] = b[:, -1] = 2
+    return p, f
+
+
+def _call_noalloc(p, f, iters: int, h2: float) -> int:
+    """Call the no-alloc entry point directly through the C ABI."""
+    nk = relax.native
+    fn = nk.lib.entry("xg_kernel_relax_noalloc")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(runtime.XGGrid), ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
+                   ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    for g in (p, f):
+        g._op_invoke(nk.depth, True)
+        g._sync_device(False)
+    device.stream().synchronize()
+    arr = (runtime.XGGrid * 2)(p.serialize(), f.serialize())
+    before = [arr[0].level[0], arr[1].level[0]]
+    packed = nk.pack([iters, h2])
+    rc = fn(arr, 2, ctypes.cast(ctypes.byref(packed), ctypes.c_void_p), ctypes.sizeof(packed), None, 0,
+            device.stream_handle())
+    device.stream().synchronize()
+    if rc == 0:
+        assert [arr[0].level[0], arr[1].level[0]] == before, "the caller's level pointers must not change"
+        for g, st in zip((p, f), arr):
+            g._adopt(st)
+    return rc
+
+
+def test_noalloc_matches_regular_entry(tmp_path):
+    xgrid.init(precision="double", cacheroot=str(tmp_path), opt_level=3)
+    n = 96
+    pa, fa = _grids(n, 11)
+    pb, fb = _grids(n, 11)
+    p0, f0 = pa.read(0), fa.read(0)
+    # one regular call builds the mask tables of pb (the no-alloc call may not);
+    # then the inputs are restored
+    relax(pb, fb, 1, 0.01)
+    pb.now[...] = p0
+    fb.now[...] = f0
+    for iters in (7, 4):  # two calls in a row; 7 leaves the result in the scratch level
+        relax(pa, fa, iters, 0.01)
+        assert _call_noalloc(pb, fb, iters, 0.01) == 0, runtime.last_error()
+        assert pa.read(0).tobytes() == pb.read(0).tobytes()
+        assert fa.read(0).tobytes() == fb.read(0).tobytes()
+
+
+def test_noalloc_refuses_to_build_tables(tmp_path):
+    xgrid.init(precision="double", cacheroot=str(tmp_path), opt_level=3)
+    warm_p, warm_f = _grids(32, 1)
+    relax(warm_p, warm_f, 1, 0.01)  # compiles the module
+    p, f = _grids(40, 2)            # fresh masks: no tables yet
+    rc = _call_noalloc(p, f, 2, 0.01)
+    assert rc != 0
+    assert "not built yet" in runtime.last_error()
+
+
+def test_noalloc_rejects_grids_beyond_the_pool(tmp_path):
+    xgrid.init(precision="double", cacheroot=str(tmp_path), opt_level=3)
+    warm_p, warm_f = _grids(32, 1)
+    relax(warm_p, warm_f, 1, 0.01)
+    p, f = _grids(3000, 3)          # 72 MB of FP64 scratch > 64 MiB
+    rc = _call_noalloc(p, f, 1, 0.01)
+    assert rc != 0
+    assert "more than the" in runtime.last_error()

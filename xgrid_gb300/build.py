@@ -19,7 +19,7 @@ LIBDIR = os.path.join(PKG, "lib")
 RUNTIME = os.path.join(LIBDIR, "libxgrid_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 RUNTIME_SOURCES = [os.path.join(CSRC, "xgrid_runtime.cu")]
-RUNTIME_DEPS = RUNTIME_SOURCES + [os.path.join(INCLUDE, "xgrid_gb300.h")]
+RUNTIME_DEPS = RUNTIME_SOURCES + [os.path.join(INCLUDE, "xgrid_gb300.h"), os.path.join(CSRC, "xgrid_internal.h")]
 
 
 def nvcc() -> str:

@@ -388,8 +388,72 @@ class CudaGenerator:
         src.append("}")
         src.append(f'extern "C" int xg_groups_{name}(void) {{ return {self.group_counter[0]}; }}')
         implicit = sorted({s.slot for s in self.sweeps if s.implicit})
+        if getattr(self.op, "noalloc", False) and grid_args and implicit:
+            src.extend(self.noalloc_entry(name, entry, grid_args, implicit))
         return Module("\n".join(src) + "\n", name, entry, self.depth + 1, grid_args, value_args, order, rtype,
                       implicit, self.group_counter[0], device_only, self.sweeps)
+
+    def noalloc_entry(self, name, entry, grid_args, implicit) -> list[str]:
+        """``<entry>_noalloc``: same computation as ``<entry>``, for callers that
+        cannot allocate device memory.  The scratch level of every grid that an
+        in-place (two-phase) sweep needs is carved out of one file-scope device
+        array; after the call, a level left in that array is copied back into
+        the caller's buffer, so the caller's level pointers never change."""
+        elems = ", ".join(f"sizeof({c_type(grid_args[s][1].element)})" for s in implicit)
+        slots = ", ".join(str(s) for s in implicit)
+        k = len(implicit)
+        pool = f"xg_noalloc_pool_{name}"
+        return [
+            "// Scratch of the no-alloc variant: a fixed pool in device memory, held by every",
+            "// GPU that loads this module until the process exits.  All calls share it.",
+            "#define XG_NOALLOC_POOL_BYTES ((size_t)64 << 20)",
+            "#define XG_NOALLOC_MAX_DEVICES 64",
+            f"static __device__ __align__(256) unsigned char {pool}[XG_NOALLOC_POOL_BYTES];",
+            f"static void* {pool}_addr[XG_NOALLOC_MAX_DEVICES];",
+            f'extern "C" int {entry}_noalloc(xg_grid* G, int ngrids, const void* args, size_t nargs, void* ret, '
+            f'size_t nret, void* stream) {{',
+            "  cudaStream_t s = (cudaStream_t)stream;",
+            f"  if (ngrids != {len(grid_args)}) XG_FAIL(\"{name}_noalloc: expected {len(grid_args)} grids, got %d\", "
+            f"ngrids);",
+            "  int dev = 0;",
+            "  XG_CUDA(cudaGetDevice(&dev));",
+            "  if (dev < 0 || dev >= XG_NOALLOC_MAX_DEVICES) XG_FAIL(\"no-alloc entry: device %d out of range\", dev);",
+            f"  if (!{pool}_addr[dev]) {{  // once per device, with that device current",
+            "    void* p = NULL;",
+            f"    XG_CUDA(cudaGetSymbolAddress(&p, {pool}));",
+            f"    {pool}_addr[dev] = p;",
+            "  }",
+            f"  unsigned char* base = (unsigned char*){pool}_addr[dev];",
+            f"  xg_grid L[{len(grid_args)}];",
+            "  memcpy(L, G, sizeof L);",
+            f"  const int slots[{k}] = {{{slots}}};",
+            f"  const size_t elem[{k}] = {{{elems}}};",
+            f"  size_t bytes[{k}], off = 0;",
+            f"  for (int i = 0; i < {k}; ++i) {{",
+            "    xg_ext e = xg_extent(&L[slots[i]]);",
+            "    bytes[i] = elem[i] * (size_t)(e.z * e.y * e.x);",
+            "    if (off + bytes[i] > XG_NOALLOC_POOL_BYTES)",
+            f"      XG_FAIL(\"{name}_noalloc: grids need %zu bytes of scratch, more than the %zu-byte pool of the "
+            f"no-alloc entry point\", off + bytes[i], (size_t)XG_NOALLOC_POOL_BYTES);",
+            "    L[slots[i]].scratch = base + off;",
+            "    off += (bytes[i] + 255) & ~(size_t)255;",
+            "  }",
+            "  xg_internal_noalloc_scope(1);",
+            f"  int rc = {entry}(L, ngrids, args, nargs, ret, nret, stream);",
+            "  xg_internal_noalloc_scope(0);",
+            "  if (rc != 0) return rc;",
+            "  // a level that ended in the pool (odd number of exchanges) goes back to the caller's buffer",
+            f"  for (int i = 0; i < {k}; ++i) {{",
+            "    const int g = slots[i];",
+            "    for (int lv = 0; lv < L[g].levels && lv < XG_MAX_LEVELS; ++lv) {",
+            "      unsigned char* q = (unsigned char*)L[g].level[lv];",
+            "      if (q >= base && q < base + XG_NOALLOC_POOL_BYTES)",
+            "        XG_CUDA(cudaMemcpyAsync(G[g].level[lv], q, bytes[i], cudaMemcpyDeviceToDevice, s));",
+            "    }",
+            "  }",
+            "  return 0;",
+            "}",
+        ]
 
     def struct_defs(self) -> list[str]:
         out = []

@@ -22,7 +22,8 @@ _lock = threading.Lock()
 
 def _header_digest() -> str:
     h = hashlib.md5()
-    for p in (os.path.join(build.CSRC, "xgrid_gen.cuh"), os.path.join(build.INCLUDE, "xgrid_gb300.h")):
+    for p in (os.path.join(build.CSRC, "xgrid_gen.cuh"), os.path.join(build.CSRC, "xgrid_internal.h"),
+              os.path.join(build.INCLUDE, "xgrid_gb300.h")):
         with open(p, "rb") as f:
             h.update(f.read())
     return h.hexdigest()

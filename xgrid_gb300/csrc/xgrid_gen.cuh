@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include "xgrid_gb300.h"
+#include "xgrid_internal.h"
 
 #define XG_HD static __host__ __device__ __forceinline__
 

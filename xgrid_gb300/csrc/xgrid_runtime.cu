@@ -23,10 +23,13 @@
 #include <vector>
 
 #include "xgrid_gb300.h"
+#include "xgrid_internal.h"
 
 namespace {
 
 thread_local std::string g_error;
+// set while a no-alloc entry point runs: building a missing table is an error
+thread_local int g_noalloc_scope = 0;
 
 int fail(const std::string& msg) {
   g_error = msg;
@@ -46,6 +49,9 @@ int cuda_fail(cudaError_t e, const char* what) {
 template <typename T>
 int upload(const std::vector<T>& host, T** dev) {
   *dev = nullptr;
+  if (g_noalloc_scope)
+    return fail("xgrid: a boundary-mask table needed by this call is not built yet, and an entry point that "
+                "may not allocate is running; make one regular call with the same grids first");
   size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(T);
   XG_CUDA(cudaMalloc(reinterpret_cast<void**>(dev), bytes));
   if (!host.empty()) XG_CUDA(cudaMemcpy(*dev, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
@@ -174,6 +180,8 @@ std::vector<uint8_t> make_key(xg_entry_fn fn, const xg_grid* g, int n, const voi
 extern "C" {
 
 const char* xg_last_error(void) { return g_error.c_str(); }
+
+void xg_internal_noalloc_scope(int on) { g_noalloc_scope = on; }
 
 void xg_set_error(const char* message) { g_error = message ? message : ""; }
 

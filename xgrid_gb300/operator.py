@@ -67,9 +67,14 @@ class Operator:
 
 
 def kernel(*, name: str | None = None, includes: list | None = None, tick: bool = True,
-           macro: list | None = None):
+           macro: list | None = None, noalloc: bool = False):
+    """``noalloc=True`` also compiles ``xg_kernel_<name>_noalloc``, a variant of
+    the module's entry point whose scratch buffers come from a fixed device pool
+    instead of the caller (see ``include/xgrid_gb300.h``)."""
     def aux(func):
-        return Operator(func, "kernel", name, includes, tick=tick, macro=macro)
+        op = Operator(func, "kernel", name, includes, tick=tick, macro=macro)
+        op.noalloc = noalloc
+        return op
     return aux
 
 
