@@ -50,7 +50,23 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help=argparse.SUPPRESS)
+    ap.add_argument("--mode", default="bench", choices=["bench", "kernels"],
+                    help="kernels: only run warm-up + steps (for profiler launch lists)")
     return ap.parse_args()
+
+
+def kernels_only(args) -> None:
+    """Set up the workload and run warm-up + steps, nothing else (profiling)."""
+    import xgrid
+    import workloads
+    from xgrid_gb300 import device
+    xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+               opt_level=3)
+    grids, cfg = workloads.cavity_setup(args.n, 1e-5)
+    for _ in range(args.warmup + args.steps):
+        workloads.cavity_kernel(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+    device.synchronize()
+    print(json.dumps({"mode": "kernels", "n": args.n, "calls": args.warmup + args.steps}))
 
 
 def peaks():
@@ -62,16 +78,25 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel_tag: str):
-    """dram bytes per launch of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
-    try:
+def profile_traffic(kernel_tag: str, n: int):
+    """DRAM bytes (read + write) per launch of the dominant kernel, from the
+    committed ncu summaries (``traffic_bytes_per_launch_<n>: <bytes>`` lines in
+    ``profiles/<kernel_tag>_*.md``).  A capture at another size is scaled by the
+    number of cells (the kernel's traffic is proportional to its cells); None
+    when no capture exists."""
+    import glob
+    found = {}
+    for path in glob.glob(os.path.join(ROOT, "profiles", f"{kernel_tag}_*.md")):
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1])
-    except OSError:
-        pass
-    return None
+            if line.startswith("traffic_bytes_per_launch_"):
+                key, val = line.split(":", 1)
+                found[int(key.rsplit("_", 1)[1])] = float(val)
+    if n in found:
+        return found[n], f"ncu capture at {n}^2"
+    if found:
+        m = max(found)
+        return found[m] * (n * n) / (m * m), f"ncu capture at {m}^2 scaled by cells"
+    return None, None
 
 
 class ClockSampler:
@@ -236,10 +261,7 @@ def gpu_bench(args, rank: int, world: int):
     alg_bytes = bytes_per_cell * n * n
     hbm_peak, peak_src = peaks()
     achieved = alg_bytes / dom_avg_s / 1e9
-    tag = "cavity_jacobi_fused_fp64"
-    traffic = profile_traffic(tag)
-    if traffic is not None:
-        traffic = traffic * (n * n) / (1025 * 1025)
+    traffic, traffic_src = profile_traffic("cavity_jacobi_fused_fp64", n)
 
     # e2e through the public API with host buffers
     for g in (u, v, p):
@@ -276,7 +298,8 @@ def gpu_bench(args, rank: int, world: int):
                    "n": n, "sweeps_per_step": SWEEPS_PER_STEP, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}", "graph": True, "launches_per_step": launches_per_step},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                     "frac": achieved / hbm_peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "peak_source": peak_src,
                      "kernel": f"group {group} (site {dom_site})", "kernel_ms": dom_avg_s * 1e3,
                      "kernel_share": sum(dom_ms) / total_prof, "algorithmic_bytes_per_launch": alg_bytes},
         "e2e": e2e,
@@ -337,6 +360,9 @@ def main():
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.mode == "kernels":
+        kernels_only(args)
+        return
     if args.impl == "reference":
         out = reference_arm(args, rank, world)
         if out is not None:

@@ -177,6 +177,9 @@ class CudaGenerator:
         sub = env.substitute(e)
         if sub is not None:
             return sub
+        div = getattr(env, "div_map", {}).get(id(e))
+        if div is not None:
+            return f"xg_divk((double)({self.expr(e.left, env)}), p.h.{div.name})"
         if isinstance(e, ir.Constant):
             return literal(e.value)
         if isinstance(e, ir.Identifier):
@@ -612,6 +615,7 @@ class Hoisted:
     name: str
     ctype: str
     expr: ir.Expression
+    divisor: bool = False  # an xg_divisor built from ``expr`` on the host
 
 
 class SweepEnv:
@@ -620,10 +624,11 @@ class SweepEnv:
 
     device = True
 
-    def __init__(self, gen, hoisted: dict, loadnames: dict) -> None:
+    def __init__(self, gen, hoisted: dict, loadnames: dict, div_map: dict | None = None) -> None:
         self.gen = gen
         self.hoisted = hoisted
         self.loadnames = loadnames
+        self.div_map = div_map or {}
 
     def substitute(self, e):
         h = self.hoisted.get(id(e))
@@ -655,6 +660,19 @@ class SweepGroupEmitter:
         self.gid = group.index
         self.hoisted: list[Hoisted] = []
         self.hoist_map: dict = {}
+        self.div_map: dict = {}
+        self.by_text: dict = {}  # (kind, host C text) -> Hoisted: equal subtrees share one parameter
+
+    def _param(self, e: ir.Expression, divisor: bool) -> "Hoisted":
+        text = self.gen.expr(e, HostEnv(self.gen))
+        key = ("k" if divisor else "v", text)
+        h = self.by_text.get(key)
+        if h is None:
+            name = f"{key[0]}{len(self.hoisted)}"
+            h = Hoisted(name, "xg_divisor" if divisor else self.gen.ctype(e), e, divisor)
+            self.hoisted.append(h)
+            self.by_text[key] = h
+        return h
 
     # ---------------------------------------------------------- hoisting
     def hoist(self, e: ir.Expression, conditional: bool = False) -> None:
@@ -665,11 +683,15 @@ class SweepGroupEmitter:
             if conditional and unsafe_int_div(e):
                 pass  # an integer division guarded by a condition stays per cell
             else:
-                h = Hoisted(f"v{len(self.hoisted)}", self.gen.ctype(e), e)
-                self.hoisted.append(h)
-                self.hoist_map[id(e)] = h
+                self.hoist_map[id(e)] = self._param(e, False)
                 return
         if isinstance(e, ir.Binary):
+            if (e.operator is ir.BinaryOperator.Div and self.gen.cfg.divisor and self.gen.ctype(e) == "double"
+                    and not has_stencil(e.right)):
+                # x / d with d fixed for the launch: precomputed reciprocal pair on the host
+                self.div_map[id(e)] = self._param(e.right, True)
+                self.hoist(e.left, conditional)
+                return
             cond = conditional or e.operator.is_logic()
             self.hoist(e.left, conditional)
             self.hoist(e.right, cond)
@@ -705,7 +727,10 @@ class SweepGroupEmitter:
         out.append(f"{indent}{{ struct xgh_{n}_{gid} h_;")
         out.append(f"{indent}  memset(&h_, 0, sizeof h_);")
         for h in self.hoisted:
-            out.append(f"{indent}  h_.{h.name} = {gen.expr(h.expr, env)};")
+            if h.divisor:
+                out.append(f"{indent}  h_.{h.name} = xg_make_divisor((double)({gen.expr(h.expr, env)}));")
+            else:
+                out.append(f"{indent}  h_.{h.name} = {gen.expr(h.expr, env)};")
         out.append(f"{indent}  XG_TRY(xgl_{n}_{gid}(G, &h_, s)); }}")
 
         launchers = []
@@ -822,7 +847,7 @@ class SweepGroupEmitter:
                 local[ld] = vn
                 lines.append(f"{indent}const {self.elem(ld.slot)} {vn} = {self.load_code(sweep, ld, fast)};")
             names[id(st)] = local[ld]
-        env = SweepEnv(self.gen, self.hoist_map, names)
+        env = SweepEnv(self.gen, self.hoist_map, names, self.div_map)
         return lines, self.gen.expr(sweep.stmt.value, env)
 
     def main_body(self, sweeps_idx: list, fast: bool, indent: str, mask_vars: dict) -> list:

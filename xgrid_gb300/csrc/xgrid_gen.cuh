@@ -46,6 +46,62 @@
 XG_HD double xg_sq_d(double a) { return a * a; }
 XG_HD float xg_sq_f(float a) { return a * a; }
 
+// ---------------------------------------------------------------------------
+// Division by a divisor known before the launch (a loop-invariant subtree).
+//
+// Method: Brisebarre, Muller & Raina, "Accelerating correctly rounded
+// floating-point division when the divisor is known in advance", IEEE Trans.
+// Computers 53(8), 2004, followed by one Markstein correction step.  With
+// zh = RN(1/d) and zl = RN(1/d - zh) precomputed on the host,
+//     q  = RN(x*zh + RN(x*zl))        within 1 ulp of x/d (a faithful quotient)
+//     r  = x - q*d                    exact (one fma) for a faithful q
+//     q' = RN(q + r*zh)               = RN(x/d) by Markstein's theorem
+// as long as nothing underflows or overflows.  The host derives from d the
+// window of x exponents where that holds; outside it (and for d not normal,
+// x = 0, inf, NaN, tiny or huge) the IEEE division runs instead, so the result
+// is RN(x/d) for every x.
+struct xg_divisor {
+  double d, zh, zl;
+  unsigned lo, span;  // fast path when (biased exponent of x) - lo <= span (unsigned)
+  int ok;
+};
+
+static inline xg_divisor xg_make_divisor(double d) {
+  xg_divisor k;
+  memset(&k, 0, sizeof k);
+  k.d = d;
+  if (!isfinite(d) || d == 0.0 || fpclassify(d) != FP_NORMAL) return k;
+  const double zh = 1.0 / d;
+  if (!isfinite(zh) || fpclassify(zh) != FP_NORMAL) return k;
+  const double e = fma(-zh, d, 1.0);  // 1 - zh*d, exact for zh = RN(1/d)
+  k.zh = zh;
+  k.zl = e / d;
+  const int ed = ilogb(d);
+  // |x| >= 2^-900 * max(1, |d|) keeps x*zl, the residual and r*zh normal;
+  // |x/d| <= 2^1000 keeps every intermediate finite.
+  int lo = -900 + (ed > 0 ? ed : 0);
+  int hi = 1000 + ed;
+  if (hi > 1023) hi = 1023;
+  if (hi < lo) return k;
+  k.lo = (unsigned)(lo + 1023);
+  k.span = (unsigned)(hi - lo);
+  k.ok = 1;
+  return k;
+}
+
+__device__ __forceinline__ double xg_divk(double x, const xg_divisor& k) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (k.ok && e - k.lo <= k.span) {
+    const double u = __dmul_rn(x, k.zl);
+    const double q = __fma_rn(x, k.zh, u);
+    const double r = __fma_rn(-q, k.d, x);
+    return __fma_rn(r, k.zh, q);
+  }
+  if ((b << 1) == 0ull && k.ok) return __dmul_rn(x, k.zh);  // +-0 / d: zero with the quotient's sign
+  return x / k.d;
+}
+
 // Collapsed (z, y, x) view of a C-order shape of 1..3 dimensions.
 struct xg_ext {
   int64_t z, y, x;
