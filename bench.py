@@ -2,7 +2,7 @@
 """Benchmark of the stencil hot path on one GB300 (or N replicas).
 
 Workload (default): the lid-driven cavity program on 1025 x 1025 FP64 grids,
-dt = 1e-5, zero initial fields; one *step* is one call of the cavity kernel
+dt = 5e-6 (see ``DT``), zero initial fields; one *step* is one call of the cavity kernel
 (1 source sweep, 1 + 50 Jacobi sweeps of the pressure with four boundary passes
 each, 2 momentum sweeps, velocity walls).  Metric: GLUP/s, counting one lattice
 update per cell per full-grid sweep (54 per step; boundary passes excluded).
@@ -36,6 +36,18 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SWEEPS_PER_STEP = 54  # b, 1 + 50 Jacobi, u, v
+# The configured dt = 1e-5 breaks the explicit-diffusion stability limit
+# nu*dt*(1/dx^2 + 1/dy^2) <= 1/2 (0.52 at 1025^2, 8.4 at 4097^2) and the fields
+# diverge after a few hundred steps; the benchmark uses the largest round dt
+# below the limit.  The work per step does not depend on dt.
+DT = {1025: 5e-6, 4097: 5e-7}
+
+
+def stable_dt(n: int) -> float:
+    if n in DT:
+        return DT[n]
+    dx = 2.0 / (n - 1)
+    return 0.2 * dx * dx / 0.1
 METRIC = "GLUP/s & HBM-roofline % per stencil: mixed/batched vs plain FP64, same GB300"
 
 
@@ -50,6 +62,9 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help=argparse.SUPPRESS)
+    ap.add_argument("--mixed-n", type=int, default=4097)
+    ap.add_argument("--mixed-steps", type=int, default=500)
+    ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mode", default="bench", choices=["bench", "kernels"],
                     help="kernels: only run warm-up + steps (for profiler launch lists)")
     return ap.parse_args()
@@ -62,7 +77,7 @@ def kernels_only(args) -> None:
     from xgrid_gb300 import device
     xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
                opt_level=3)
-    grids, cfg = workloads.cavity_setup(args.n, 1e-5)
+    grids, cfg = workloads.cavity_setup(args.n, stable_dt(args.n))
     for _ in range(args.warmup + args.steps):
         workloads.cavity_kernel(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
     device.synchronize()
@@ -156,7 +171,7 @@ def cpu_sample(n: int, steps: int) -> dict:
         kind = "port"
         o = native.Oracle("port")
     f = native.cavity_fields(n)
-    cfg = (1.0, 0.1, 1e-5, 2.0 / (n - 1), 2.0 / (n - 1))
+    cfg = (1.0, 0.1, stable_dt(n), 2.0 / (n - 1), 2.0 / (n - 1))
     o.cavity(f, cfg, 1)  # warm-up (page faults, thread team)
     t0 = time.perf_counter()
     o.cavity(f, cfg, steps)
@@ -195,7 +210,7 @@ def gpu_bench(args, rank: int, world: int):
     cache = os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}")
     xgrid.init(precision="double", cacheroot=cache, opt_level=3)
     n = args.n
-    grids, cfg = workloads.cavity_setup(n, 1e-5)
+    grids, cfg = workloads.cavity_setup(n, stable_dt(n))
     kern = workloads.cavity_kernel
     b, p, u, v = grids["b"], grids["p"], grids["u"], grids["v"]
 
@@ -293,8 +308,8 @@ def gpu_bench(args, rank: int, world: int):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic: zero initial fields, lid u=1 (deterministic)",
-        "config": {"workload": f"lid-driven cavity {n}x{n} FP64 plain, dt=1e-5, 50+1 Jacobi sweeps/step, "
-                               f"bit-exact vs reference C",
+        "config": {"workload": f"lid-driven cavity {n}x{n} FP64 plain, dt={stable_dt(n):g}, 50+1 Jacobi "
+                               f"sweeps/step, bit-exact vs reference C",
                    "n": n, "sweeps_per_step": SWEEPS_PER_STEP, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}", "graph": True, "launches_per_step": launches_per_step},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -307,6 +322,54 @@ def gpu_bench(args, rank: int, world: int):
         "clocks": clk.summary(),
     }
     return result
+
+
+def mixed_section(n: int, steps: int) -> dict:
+    """Cavity at n^2 for ``steps`` steps: plain FP64 vs FP32 defect iterations with
+    FP64 residual/correction (``mixed="fp32"``), same initial state; steps/s of
+    each (CUDA events over the second half of the run; fields exceed L2) and the
+    error of p, u, v against the FP64 run."""
+    import numpy as np
+    import torch
+
+    import xgrid
+    import workloads
+    from xgrid_gb300 import device
+    from xgrid_gb300.operator import Operator
+
+    dt = stable_dt(n)
+    out, fields = {}, {}
+    for mode in (None, "fp32"):
+        xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+                   opt_level=3, mixed=mode)
+        k = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
+        grids, cfg = workloads.cavity_setup(n, dt)
+        args = (grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+        half = steps // 2
+        for _ in range(steps - half):
+            k(*args)
+        s = device.stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(half):
+            k(*args)
+        e1.record(s)
+        s.synchronize()
+        ms = e0.elapsed_time(e1) / half
+        fields[mode] = {g: grids[g].read(0) for g in "puv"}
+        out["fp64" if mode is None else mode] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms,
+                                                 "value": SWEEPS_PER_STEP * n * n / (ms * 1e-3) / 1e9,
+                                                 "unit": "GLUP/s"}
+    err = {}
+    for g in "puv":
+        a, ref = fields["fp32"][g], fields[None][g]
+        err[g] = {"max_rel": float(np.abs(a - ref).max() / np.abs(ref).max()),
+                  "l2_rel": float(np.linalg.norm(a - ref) / np.linalg.norm(ref))}
+    out["fp32"]["error_vs_fp64"] = err
+    out["fp32"]["speedup_vs_fp64"] = out["fp64"]["ms_per_step"] / out["fp32"]["ms_per_step"]
+    out["config"] = f"cavity {n}x{n}, dt={dt:g}, {steps} steps from zero fields; FP32 defect sweeps, " \
+                    f"FP64 source, residual, correction and projection; one correction per 50-iteration loop"
+    return out
 
 
 def algorithmic_bytes(module, group: int) -> float:
@@ -345,7 +408,8 @@ def reference_arm(args, rank: int, world: int):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["seconds"] / r["steps"] * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: zero initial fields, lid u=1 (deterministic)",
-        "config": {"workload": f"lid-driven cavity {n}x{n} FP64 plain, dt=1e-5, 50+1 Jacobi sweeps/step", "n": n,
+        "config": {"workload": f"lid-driven cavity {n}x{n} FP64 plain, dt={stable_dt(n):g}, 50+1 Jacobi "
+                               f"sweeps/step", "n": n,
                    "sweeps_per_step": SWEEPS_PER_STEP},
         "cpu_baseline": {"value": val, "unit": "GLUP/s", "cores": r["cores"], "kind": r["kind"],
                          "sample": f"cavity {n}x{n} FP64, {r['steps']} steps ({r['seconds']:.1f} s)"},
@@ -373,6 +437,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
     out = gpu_bench(args, rank, world)
+    if rank == 0 and not args.no_mixed:
+        out["mixed"] = mixed_section(args.mixed_n, args.mixed_steps)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)

@@ -56,6 +56,9 @@ typedef struct xg_grid {
     void* scratch;                 /* device buffer of one level, exchanged with
                                       level[0] by two-phase sweeps (may be NULL)      */
     xg_mask* mask;                 /* boundary mask handle                            */
+    void* aux;                     /* device work area of mixed-precision loops
+                                      (defect and residual fields; may be NULL)       */
+    int64_t aux_bytes;             /* size of aux                                     */
 } xg_grid;
 
 /*
@@ -105,8 +108,10 @@ int xg_runtime_version(void);
  * grid's shape whose value k selects the `with xgrid.boundary(k)` sweeps that
  * update a cell (xgrid/lang/generator.py:295-298). */
 int xg_mask_create(int ndim, const int64_t* shape, xg_mask** out);
+/* Frees the mask and its tables; drops every cached graph first. */
 int xg_mask_destroy(xg_mask* mask);
-/* Copy a host mask in, rebuild the per-value cell lists, upload (synchronous). */
+/* Copy a host mask in, rebuild the per-value cell lists, upload (synchronous).
+ * Every upload gets a version number that is unique in the process. */
 int xg_mask_upload(xg_mask* mask, const int32_t* host);
 uint64_t xg_mask_version(const xg_mask* mask);
 const int32_t* xg_mask_device(const xg_mask* mask);

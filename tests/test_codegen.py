@@ -1,0 +1,64 @@
+"""Generator, grouping and mixed-precision matching on the CPU (no GPU needed;
+the generated CUDA is compiled by nvcc for sm_103a where nvcc is present)."""
+import shutil
+
+import pytest
+
+import xgrid
+import workloads
+from xgrid_gb300 import analysis, mixed
+from xgrid_gb300.codegen import CudaGenerator
+from xgrid_gb300.config import get_config
+from xgrid_gb300.operator import Operator
+
+
+def _gen(op, **cfg):
+    xgrid.init(precision="double", cacheroot="/tmp/xgcg", opt_level=3, **cfg)
+    return CudaGenerator(Operator(op.func, "kernel", op.name), get_config()).generate()
+
+
+def test_cavity_groups_and_launches():
+    m = _gen(workloads.cavity_kernel)
+    assert m.depth == 2
+    assert m.groups == 3
+    assert m.implicit_slots == [1]
+    groups = {}
+    for s in m.sweeps:
+        groups.setdefault(s.group_index, []).append(s)
+    # b + first p sweep + 4 boundaries | Jacobi + 4 boundaries | u + v + 3 walls
+    assert [len(groups[i]) for i in sorted(groups)] == [6, 5, 5]
+    jac = groups[1]
+    assert jac[0].implicit and jac[0].write_version == 1
+    assert all(s.mask != 0 for s in jac[1:])
+
+
+def test_divisors_are_precomputed_and_deduplicated():
+    m = _gen(workloads.cavity_kernel)
+    assert "xg_divk(" in m.source
+    # 2.0*cfg.dx, 2.0*cfg.dy, 2*(dx^2+dy^2), dx, dy: one parameter each per group
+    assert m.source.count("xg_make_divisor((double)((2.0 * (cfg).dx)))") == 1
+    m2 = _gen(workloads.cavity_kernel, divisor=False)
+    assert "xg_divk(" not in m2.source.split("struct xga_")[1]
+
+
+def test_mixed_matches_cavity_pressure_loop():
+    m = _gen(workloads.cavity_kernel, mixed="fp32")
+    assert m.aux_per_cell == {1: 12}
+    assert "_mxd(" in m.source and "_mxc(" in m.source
+
+
+def test_affine_degree():
+    xgrid.init(precision="double", cacheroot="/tmp/xgcg", opt_level=3)
+    defn = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel").ir
+    loop = next(s for s in defn.body if s.__class__.__name__ == "For")
+    assert mixed.degree(loop.body[0].value, "p") == 1
+    assert all(mixed.degree(s.value, "p") in (0, 1) for s in loop.body[1:])
+    assert mixed.degree(defn.body[0].value, "p") == 0  # the source term does not read p
+
+
+@pytest.mark.skipif(shutil.which("nvcc") is None, reason="nvcc not available")
+def test_generated_modules_compile():
+    from xgrid_gb300.compiler import Compiler
+    for kw in ({}, {"mixed": "fp32"}):
+        m = _gen(workloads.cavity_kernel, **kw)
+        Compiler(cacheroot="/tmp/xgcg").compile(m.source, get_config().nvcc_flags)

@@ -44,7 +44,20 @@ from .types import (Boolean, Floating, GridType, Ignore, Integer, Pointer, Struc
 OVERSTEP = {"none": "XG_OVERSTEP_NONE", "limit": "XG_OVERSTEP_LIMIT", "wrap": "XG_OVERSTEP_WRAP"}
 
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
-DEFAULT_TILING = {1: (1, 1, 256, 256, 1, 1), 2: (1, 8, 32, 32, 8, 1), 3: (1, 8, 32, 32, 8, 1)}
+DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 32, 32, 32, 8, 1), 3: (1, 16, 32, 32, 8, 1)}
+
+# tile prologue and cell loop shared by the tile kernels (32-bit coordinates,
+# 64-bit linear index per row)
+TILE_PROLOGUE = ["  const xg_tile T = xg_tile_of(p.Z, p.Y, p.X, p.tz, p.ty, p.tx, p.nty, p.ntx, p.ntz);",
+                 "  const int64_t t = T.t;",
+                 "  const int z0 = T.z0, z1 = T.z1, y0 = T.y0, y1 = T.y1, x0 = T.x0, x1 = T.x1;",
+                 "  const int64_t sy = p.X, sz = p.X * p.Y;",
+                 "  (void)sy; (void)sz; (void)t;"]
+CELL_LOOP = ["  for (int z = z0; z < z1; ++z)",
+             "  for (int y = y0 + (int)threadIdx.y; y < y1; y += (int)blockDim.y) {",
+             "    const int64_t row_ = ((int64_t)z * p.Y + y) * p.X;",
+             "    for (int x = x0 + (int)threadIdx.x; x < x1; x += (int)blockDim.x) {",
+             "    const int64_t c = row_ + x;"]
 
 _INT_RANK = {"bool": 0, "int8_t": 1, "int16_t": 2, "int": 3, "int32_t": 3, "int64_t": 4}
 
@@ -110,6 +123,7 @@ class Module:
     arg_order: list          # ("grid"|"value", index) per declared argument
     return_type: object
     implicit_slots: list     # grid slots that need a scratch buffer
+    aux_per_cell: dict       # grid slot -> bytes per cell of the mixed-precision work area
     groups: int
     device_only: bool        # kernel has no grid arguments (body runs on the device)
     sweeps: list             # analysis.Sweep per grid assignment (for the oracle and tests)
@@ -130,6 +144,8 @@ class CudaGenerator:
         self.group_counter = [0]
         self.group_tiling: dict = {}
         self.sweeps: list = []
+        self.mixed_slots: dict = {}   # grid slot -> aux bytes per cell of mixed-precision loops
+        self._plans: dict = {}
         self.slots = analysis.grid_slots(self.defn)
         self.grid_names = {name: i for name, i in self.slots.items()}
         self.mode = OVERSTEP[config.overstep]
@@ -300,6 +316,16 @@ class CudaGenerator:
                 out.append(f"{indent}while ({self.expr(s.condition, env)}) {{")
                 self.block(s.body, env, indent + "  ", out, ret_mode)
                 out.append(f"{indent}}}")
+            elif isinstance(s, ir.For) and self.mixed_plan(s) is not None:
+                from .mixed import MixedLoopEmitter
+                plan = self.mixed_plan(s)
+                for sw in plan.group.sweeps:
+                    for st, _ in sw.loads:
+                        self.depth = max(self.depth, abs(st.time_offset))
+                    self.depth = max(self.depth, sw.level)
+                self.sweeps.extend(plan.group.sweeps)
+                self.mixed_slots[plan.slot] = 12
+                MixedLoopEmitter(self, plan).emit(env, indent, out)
             elif isinstance(s, ir.For):
                 v = s.variable.name
                 out.append(f"{indent}for ({v} = {self.expr(s.start, env)}; {v} < {self.expr(s.end, env)}; "
@@ -308,6 +334,18 @@ class CudaGenerator:
                 out.append(f"{indent}}}")
             else:
                 raise TypeError(f"cannot emit statement {type(s).__name__}")
+
+    def mixed_plan(self, loop: ir.For):
+        if self.cfg.mixed is None:
+            return None
+        if id(loop) not in self._plans:
+            from . import mixed
+            plan = mixed.match(self, loop)
+            if plan is not None and not all(mixed.coefficients_stencil_free(sw.stmt.value, plan.target)
+                                            for sw in plan.group.sweeps):
+                plan = None
+            self._plans[id(loop)] = plan
+        return self._plans[id(loop)]
 
     # ================================================================ sweeps
     def emit_run(self, run: list, env, indent: str, out: list) -> None:
@@ -376,6 +414,7 @@ class CudaGenerator:
             src.append("  char xg_empty;")
         src.append("};")
         src.append(f"static int xg_fuse_{name} = {1 if self.cfg.fuse else 0};")
+        src.append(f"static int64_t xg_mixed_every_{name} = {int(self.cfg.mixed_every)};")
         src.append(f"static int32_t xg_tiling_{name}[{max(self.group_counter[0], 1)}][6] = {{")
         for gi in range(max(self.group_counter[0], 1)):
             src.append("  {" + ", ".join(str(v) for v in self.group_tiling.get(gi, DEFAULT_TILING[2])) + "},")
@@ -390,11 +429,12 @@ class CudaGenerator:
         src.append("  return 0;")
         src.append("}")
         src.append(f'extern "C" int xg_groups_{name}(void) {{ return {self.group_counter[0]}; }}')
+        src.append(f'extern "C" int xg_mixed_{name}(int64_t every) {{ xg_mixed_every_{name} = every; return 0; }}')
         implicit = sorted({s.slot for s in self.sweeps if s.implicit})
         if getattr(self.op, "noalloc", False) and grid_args and implicit:
             src.extend(self.noalloc_entry(name, entry, grid_args, implicit))
         return Module("\n".join(src) + "\n", name, entry, self.depth + 1, grid_args, value_args, order, rtype,
-                      implicit, self.group_counter[0], device_only, self.sweeps)
+                      implicit, dict(self.mixed_slots), self.group_counter[0], device_only, self.sweeps)
 
     def noalloc_entry(self, name, entry, grid_args, implicit) -> list[str]:
         """``<entry>_noalloc``: same computation as ``<entry>``, for callers that
@@ -711,12 +751,30 @@ class SweepGroupEmitter:
 
     # ----------------------------------------------------------- emission
     def emit(self, env: HostEnv, indent: str, out: list) -> None:
-        gen = self.gen
+        self.prepare()
+        out.append(f"{indent}{{")
+        out.extend(self.host_hoists(env, indent + "  "))
+        out.append(f"{indent}  XG_TRY(xgl_{self.name}_{self.gid}(G, &h_, s));")
+        out.append(f"{indent}}}")
+        self.emit_kernels()
+
+    def prepare(self) -> None:
         for s in self.g.sweeps:
             self.hoist(s.stmt.value)
-        n = self.name
-        gid = self.gid
-        # hoisted values struct + their host evaluation
+
+    def host_hoists(self, env, indent: str) -> list:
+        """Host lines declaring ``h_`` and evaluating every hoisted subtree."""
+        gen, n, gid = self.gen, self.name, self.gid
+        out = [f"{indent}struct xgh_{n}_{gid} h_;", f"{indent}memset(&h_, 0, sizeof h_);"]
+        for h in self.hoisted:
+            if h.divisor:
+                out.append(f"{indent}h_.{h.name} = xg_make_divisor((double)({gen.expr(h.expr, env)}));")
+            else:
+                out.append(f"{indent}h_.{h.name} = {gen.expr(h.expr, env)};")
+        return out
+
+    def emit_kernels(self) -> None:
+        gen, n, gid = self.gen, self.name, self.gid
         hs = [f"struct xgh_{n}_{gid} {{"]
         for h in self.hoisted:
             hs.append(f"  {h.ctype} {h.name};")
@@ -724,25 +782,13 @@ class SweepGroupEmitter:
             hs.append("  char xg_empty;")
         hs.append("};")
         gen.device_chunks.append("\n".join(hs))
-        out.append(f"{indent}{{ struct xgh_{n}_{gid} h_;")
-        out.append(f"{indent}  memset(&h_, 0, sizeof h_);")
-        for h in self.hoisted:
-            if h.divisor:
-                out.append(f"{indent}  h_.{h.name} = xg_make_divisor((double)({gen.expr(h.expr, env)}));")
-            else:
-                out.append(f"{indent}  h_.{h.name} = {gen.expr(h.expr, env)};")
-        out.append(f"{indent}  XG_TRY(xgl_{n}_{gid}(G, &h_, s)); }}")
-
-        launchers = []
         if self.g.fusable:
             self.emit_fused()
-            launchers.append("fused")
         for j, s in enumerate(self.g.sweeps):
             if s.is_main:
                 self.emit_main_single(j, s)
             else:
                 self.emit_bnd_single(j, s)
-        # dispatcher
         lines = [f"static int xgl_{n}_{gid}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s) {{"]
         if self.g.fusable:
             lines += [f"  if (xg_fuse_{n}) {{",
@@ -873,7 +919,7 @@ class SweepGroupEmitter:
             lines.append(f"{indent}}}")
         return lines
 
-    def main_kernel(self, tag: str, mains: list, bnd_phases: list) -> str:
+    def main_kernel(self, tag: str, mains: list, bnd_phases: list, final: list | None = None) -> str:
         """Tile kernel: main sweeps ``mains`` (indices into the group) then the
         boundary phases ``bnd_phases`` on the tile's own cells."""
         n, gid = self.name, self.gid
@@ -887,33 +933,21 @@ class SweepGroupEmitter:
                     lo[a] = min(lo[a], ld.offset[a])
                     hi[a] = max(hi[a], ld.offset[a])
         lines = [f"__global__ void __launch_bounds__(1024) xgk_{n}_{gid}_{tag}(const __grid_constant__ "
-                 f"struct xgp_{n}_{gid}_{tag} p) {{",
-                 "  const int64_t t = blockIdx.x;",
-                 "  const int64_t itx = t % p.ntx, ity = (t / p.ntx) % p.nty, itz = t / (p.ntx * p.nty);",
-                 "  int64_t z0, z1, y0, y1, x0, x1;",
-                 "  xg_tile_range(p.Z, p.tz, p.ntz, itz, &z0, &z1);",
-                 "  xg_tile_range(p.Y, p.ty, p.nty, ity, &y0, &y1);",
-                 "  xg_tile_range(p.X, p.tx, p.ntx, itx, &x0, &x1);",
-                 "  const int64_t sy = p.X, sz = p.X * p.Y;",
-                 "  (void)sy; (void)sz;",
+                 f"struct xgp_{n}_{gid}_{tag} p) {{"] + TILE_PROLOGUE + [
                  f"  const bool fast = p.same && z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && "
                  f"y0 + ({lo[1]}) >= 0 && y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;"]
         mask_vars = {}
         for j in mains:
             mask_vars[j] = f"mz{j}"
             lines.append(f"  const bool mz{j} = p.tzero{j}[t] != 0;")
-        loop_head = ["  for (int64_t z = z0; z < z1; ++z)",
-                     "  for (int64_t y = y0 + threadIdx.y; y < y1; y += blockDim.y)",
-                     "  for (int64_t x = x0 + threadIdx.x; x < x1; x += blockDim.x) {",
-                     "    const int64_t c = (z * p.Y + y) * p.X + x;"]
         lines.append("  if (fast) {")
-        lines += ["  " + l for l in loop_head]
+        lines += ["  " + l for l in CELL_LOOP]
         lines += self.main_body(mains, True, "      ", mask_vars)
-        lines.append("    }")
+        lines.append("    }}")
         lines.append("  } else {")
-        lines += ["  " + l for l in loop_head]
+        lines += ["  " + l for l in CELL_LOOP]
         lines += self.main_body(mains, False, "      ", mask_vars)
-        lines.append("    }")
+        lines.append("    }}")
         lines.append("  }")
         for j in bnd_phases:
             s = self.g.sweeps[j]
@@ -931,6 +965,10 @@ class SweepGroupEmitter:
             lines += pre
             lines.append(f"    p.{dst}[c] = {val};")
             lines += ["    }", "  }"]
+        if final:
+            lines += ["  __syncthreads();"] + CELL_LOOP
+            lines += ["    " + l for l in final]
+            lines.append("  }}")
         lines.append("}")
         return "\n".join(lines)
 
@@ -985,9 +1023,10 @@ class SweepGroupEmitter:
             L.append(f"  XG_CUDA(cudaMemcpyAsync(p.{dst}, p.{src}, (size_t)(p.e{s.slot}[0] * p.e{s.slot}[1] * "
                      f"p.e{s.slot}[2]) * sizeof(*p.{dst}), cudaMemcpyDeviceToDevice, s));")
         site = gid * 64 + j
-        L += ["  dim3 block(tl[3], tl[4], tl[5]);",
+        L += ["  dim3 block(tl[3], tl[4], tl[5]), grid;",
+              "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
               f"  xg_prof_launch({site}, s);",
-              f"  xgk_{n}_{gid}_{tag}<<<(unsigned)ntiles, block, 0, s>>>(p);",
+              f"  xgk_{n}_{gid}_{tag}<<<grid, block, 0, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
               f"  xg_prof_end({site}, s);"]
         if s.implicit:
@@ -1035,23 +1074,28 @@ class SweepGroupEmitter:
               "  return 0;", "}"]
         self.gen.host_chunks.append("\n".join(L))
 
-    def emit_fused(self) -> None:
+    def emit_fused(self, tag: str = "fused", extra_params: list | None = None, extra_args: str = "",
+                   extra_fill: list | None = None, final: list | None = None, swap: bool = True) -> None:
+        """Fused launch of the whole group.  The variant hooks (extra parameters,
+        a final per-cell phase, no level exchange) serve the mixed-precision
+        residual launch."""
         n, gid = self.name, self.gid
-        tag = "fused"
         sweeps = self.g.sweeps
         mains = [j for j, s in enumerate(sweeps) if s.is_main]
         bnds = [j for j, s in enumerate(sweeps) if not s.is_main]
-        extra = []
+        extra = list(extra_params or [])
         for j in mains:
             extra += [f"const int32_t* m{j}", f"const uint8_t* tzero{j}"]
         for j in bnds:
             extra += [f"const int32_t* bo{j}", f"const int64_t* bc{j}"]
         self.gen.device_chunks.append(self.params_struct(tag, sweeps, extra))
-        self.gen.device_chunks.append(self.main_kernel(tag, mains, bnds))
+        self.gen.device_chunks.append(self.main_kernel(tag, mains, bnds, final))
         dom = sweeps[mains[0]].slot
-        L = [f"static int xgl_{n}_{gid}_{tag}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s) {{"]
+        L = [f"static int xgl_{n}_{gid}_{tag}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s"
+             f"{extra_args}) {{"]
         L += self.check_levels(sweeps)
         L += self.fill_params(tag, sweeps, dom)
+        L += list(extra_fill or [])
         for j in mains + bnds:
             L.append(f"  if (!xg_same_ext(xg_extent(&G[{sweeps[j].slot}]), dom)) return 0;")
         L.append("  int64_t ntiles = 0;")
@@ -1070,13 +1114,14 @@ class SweepGroupEmitter:
                   f"xg_overstep, &ok));",
                   "    if (!ok) return 0;", "  }"]
         L += ["  if (ntiles != p.ntz * p.nty * p.ntx) XG_FAIL(\"tile table mismatch\");",
-              "  dim3 block(tl[3], tl[4], tl[5]);",
-              f"  xg_prof_launch({gid * 64 + 63}, s);",
-              f"  xgk_{n}_{gid}_{tag}<<<(unsigned)ntiles, block, 0, s>>>(p);",
+              "  dim3 block(tl[3], tl[4], tl[5]), grid;",
+              "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
+              f"  xg_prof_launch({gid * 64 + 63 if swap else gid * 64 + 62}, s);",
+              f"  xgk_{n}_{gid}_{tag}<<<grid, block, 0, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
-              f"  xg_prof_end({gid * 64 + 63}, s);"]
+              f"  xg_prof_end({gid * 64 + 63 if swap else gid * 64 + 62}, s);"]
         for s in sweeps:
-            if s.implicit:
+            if s.implicit and swap:
                 L.append(f"  {{ void* t_ = G[{s.slot}].level[{s.level}]; G[{s.slot}].level[{s.level}] = "
                          f"G[{s.slot}].scratch; G[{s.slot}].scratch = t_; }}")
         L += ["  return 1;", "}"]

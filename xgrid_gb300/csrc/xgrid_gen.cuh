@@ -171,3 +171,35 @@ __device__ __forceinline__ void xg_tile_range(int64_t n, int32_t t, int64_t nt, 
 }
 
 static inline int64_t xg_tiles_along(int64_t n, int32_t t) { return n / t > 0 ? n / t : 1; }
+
+// The tile of the calling CTA: the launch grid is (ntx, nty, ntz) tiles, so the
+// tile coordinates are the block indices (no division); t is the linear tile id
+// used by the mask tables.
+struct xg_tile {
+  int z0, z1, y0, y1, x0, x1;
+  int64_t t;
+};
+
+__device__ __forceinline__ xg_tile xg_tile_of(int64_t Z, int64_t Y, int64_t X, int tz, int ty, int tx,
+                                              int64_t nty, int64_t ntx, int64_t ntz) {
+  xg_tile T;
+  const int ix = blockIdx.x, iy = blockIdx.y, iz = blockIdx.z;
+  T.t = ((int64_t)iz * nty + iy) * ntx + ix;
+  T.x0 = ix * tx;
+  T.x1 = (ix == ntx - 1) ? (int)X : (ix + 1) * tx;
+  T.y0 = iy * ty;
+  T.y1 = (iy == nty - 1) ? (int)Y : (iy + 1) * ty;
+  T.z0 = iz * tz;
+  T.z1 = (iz == ntz - 1) ? (int)Z : (iz + 1) * tz;
+  return T;
+}
+
+// Launch grid of a tiling; fails when an axis exceeds what CUDA allows.
+static inline int xg_tile_grid(int64_t ntx, int64_t nty, int64_t ntz, dim3* grid) {
+  if (ntx > 2147483647LL || nty > 65535 || ntz > 65535) {
+    xg_set_error("tiling needs more than 65535 tiles along y or z; use larger tiles");
+    return -1;
+  }
+  *grid = dim3((unsigned)ntx, (unsigned)nty, (unsigned)ntz);
+  return 0;
+}

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -28,6 +29,9 @@
 namespace {
 
 thread_local std::string g_error;
+// Mask versions are unique in the process: a new mask (whose handle and level
+// buffers may reuse freed addresses) can never match a cached graph of an old one.
+std::atomic<uint64_t> g_mask_versions{0};
 // set while a no-alloc entry point runs: building a missing table is an error
 thread_local int g_noalloc_scope = 0;
 
@@ -169,6 +173,7 @@ std::vector<uint8_t> make_key(xg_entry_fn fn, const xg_grid* g, int n, const voi
     put(g[i].level, sizeof(g[i].level));
     put(&g[i].scratch, sizeof(void*));
     put(&g[i].mask, sizeof(void*));
+    put(&g[i].aux, sizeof(void*));
     uint64_t v = g[i].mask ? g[i].mask->version : 0;
     put(&v, sizeof(v));
   }
@@ -178,6 +183,8 @@ std::vector<uint8_t> make_key(xg_entry_fn fn, const xg_grid* g, int n, const voi
 }  // namespace
 
 extern "C" {
+
+int xg_graph_clear(xg_entry_fn fn);
 
 const char* xg_last_error(void) { return g_error.c_str(); }
 
@@ -208,6 +215,10 @@ int xg_mask_create(int ndim, const int64_t* shape, xg_mask** out) {
 
 int xg_mask_destroy(xg_mask* m) {
   if (!m) return 0;
+  // cached graphs may reference this mask's tables: drop them, and let work in
+  // flight finish, before freeing
+  xg_graph_clear(nullptr);
+  cudaDeviceSynchronize();
   m->release_tables();
   cudaFree(m->dev);
   delete m;
@@ -223,7 +234,7 @@ int xg_mask_upload(xg_mask* m, const int32_t* host) {
     if (m->host[i] != 0) m->cells[m->host[i]].push_back(i);
   if (!m->dev) XG_CUDA(cudaMalloc(reinterpret_cast<void**>(&m->dev), m->total * sizeof(int32_t)));
   XG_CUDA(cudaMemcpy(m->dev, m->host.data(), m->total * sizeof(int32_t), cudaMemcpyHostToDevice));
-  m->version += 1;
+  m->version = ++g_mask_versions;
   return 0;
 }
 

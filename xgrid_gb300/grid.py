@@ -58,6 +58,7 @@ class Grid:
         self._mask_uploaded = None
         self._mask = None
         self._scratch = None
+        self._aux = None
         self._nbytes = int(np.prod(self.shape)) * self.numpy_dtype.itemsize
 
     # ------------------------------------------------------------ reference API
@@ -150,7 +151,7 @@ class Grid:
             lv.auth = "host"
         return lv.host
 
-    def _sync_device(self, need_scratch: bool) -> bool:
+    def _sync_device(self, need_scratch: bool, aux_bytes: int = 0) -> bool:
         """Allocate and upload what the device lacks; True when host data was
         uploaded (the caller then waits for the copies before returning, so the
         host arrays handed out earlier can be modified again safely)."""
@@ -171,6 +172,8 @@ class Grid:
                 uploaded = True
         if need_scratch and self._scratch is None:
             self._scratch = device.alloc_bytes(self._nbytes)
+        if aux_bytes and (self._aux is None or self._aux.numel() < aux_bytes):
+            self._aux = device.alloc_bytes(aux_bytes)
         if self._mask_dirty or self._mask is None:
             self._upload_mask()
         return uploaded
@@ -200,6 +203,8 @@ class Grid:
             g.level[i] = lv.dev.data_ptr()
         g.scratch = self._scratch.data_ptr() if self._scratch is not None else None
         g.mask = self._mask
+        g.aux = self._aux.data_ptr() if self._aux is not None else None
+        g.aux_bytes = self._aux.numel() if self._aux is not None else 0
         return g
 
     def _adopt(self, g: runtime.XGGrid) -> None:

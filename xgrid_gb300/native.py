@@ -11,6 +11,8 @@ from __future__ import annotations
 
 import ctypes
 
+import numpy as np
+
 from . import device, runtime
 from .codegen import CudaGenerator
 from .compiler import Compiler, Library
@@ -42,6 +44,15 @@ class NativeKernel:
         self.scratch_slots = set(self.module.implicit_slots)
         self.nargs = len(self.module.arg_order)
         self.use_graph = self.config.graph and not self.module.device_only
+        self.mixed_fn = getattr(self.lib.dylib, f"xg_mixed_{self.module.name}", None)
+        if self.mixed_fn is not None:
+            self.mixed_fn.argtypes = [ctypes.c_int64]
+            self.mixed_fn.restype = ctypes.c_int
+
+    def set_mixed_every(self, every: int) -> None:
+        """Iterations between FP64 corrections of mixed-precision loops (0 = once per loop)."""
+        self.mixed_fn(int(every))
+        runtime.load().xg_graph_clear(self.fn_ptr)
 
     # ---------------------------------------------------------------- tuning
     def set_tiling(self, group: int, tiling: tuple) -> None:
@@ -78,7 +89,8 @@ class NativeKernel:
             g._op_invoke(self.depth, self.op.tick)
         uploaded = False
         for i, g in enumerate(grids):
-            uploaded |= g._sync_device(i in self.scratch_slots)
+            aux = self.module.aux_per_cell.get(i, 0) * int(np.prod(g.shape))
+            uploaded |= g._sync_device(i in self.scratch_slots, aux)
         if uploaded:
             device.stream().synchronize()
         packed = self.pack(values)

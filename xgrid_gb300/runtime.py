@@ -21,7 +21,9 @@ class XGGrid(ctypes.Structure):
                 ("shape", ctypes.c_int64 * XG_MAX_DIM),
                 ("level", ctypes.c_void_p * XG_MAX_LEVELS),
                 ("scratch", ctypes.c_void_p),
-                ("mask", ctypes.c_void_p)]
+                ("mask", ctypes.c_void_p),
+                ("aux", ctypes.c_void_p),
+                ("aux_bytes", ctypes.c_int64)]
 
 
 ENTRY_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(XGGrid), ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
