@@ -65,6 +65,8 @@ def parse_args():
     ap.add_argument("--mixed-n", type=int, default=4097)
     ap.add_argument("--mixed-steps", type=int, default=500)
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mixed", default=None, choices=[None, "fp32", "fp16", "bf16"],
+                    help="kernels mode: precision lowering of the pressure loop")
     ap.add_argument("--mode", default="bench", choices=["bench", "kernels"],
                     help="kernels: only run warm-up + steps (for profiler launch lists)")
     return ap.parse_args()
@@ -76,7 +78,7 @@ def kernels_only(args) -> None:
     import workloads
     from xgrid_gb300 import device
     xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
-               opt_level=3)
+               opt_level=3, mixed=args.mixed)
     grids, cfg = workloads.cavity_setup(args.n, stable_dt(args.n))
     for _ in range(args.warmup + args.steps):
         workloads.cavity_kernel(grids["b"], grids["p"], grids["u"], grids["v"], cfg)

@@ -51,13 +51,14 @@ DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 32, 32, 32, 8, 1), 3: (1, 1
 TILE_PROLOGUE = ["  const xg_tile T = xg_tile_of(p.Z, p.Y, p.X, p.tz, p.ty, p.tx, p.nty, p.ntx, p.ntz);",
                  "  const int64_t t = T.t;",
                  "  const int z0 = T.z0, z1 = T.z1, y0 = T.y0, y1 = T.y1, x0 = T.x0, x1 = T.x1;",
-                 "  const int64_t sy = p.X, sz = p.X * p.Y;",
+                 "  const I sy = (I)p.X, sz = (I)(p.X * p.Y);",
                  "  (void)sy; (void)sz; (void)t;"]
+# I is the kernel's index type: int when the grid has fewer than 2^31 cells
 CELL_LOOP = ["  for (int z = z0; z < z1; ++z)",
              "  for (int y = y0 + (int)threadIdx.y; y < y1; y += (int)blockDim.y) {",
-             "    const int64_t row_ = ((int64_t)z * p.Y + y) * p.X;",
+             "    const I row_ = (I)z * sz + (I)y * sy;",
              "    for (int x = x0 + (int)threadIdx.x; x < x1; x += (int)blockDim.x) {",
-             "    const int64_t c = row_ + x;"]
+             "    const I c = row_ + (I)x;"]
 
 _INT_RANK = {"bool": 0, "int8_t": 1, "int16_t": 2, "int": 3, "int32_t": 3, "int64_t": 4}
 
@@ -855,6 +856,14 @@ class SweepGroupEmitter:
                 out.append(b[0])
         return out
 
+    def restrict_locals(self, sweeps) -> list:
+        """Kernel-local __restrict__ copies of the buffer pointers: distinct buffer
+        names never alias (a grid is passed once; levels and scratch are separate
+        allocations), which lets the compiler issue the loads of several cells
+        before their stores."""
+        return [f"  {self.elem(b[0])}* __restrict__ {self.bname(b)} = p.{self.bname(b)};"
+                for b in self.buffers(sweeps)]
+
     def params_struct(self, tag: str, sweeps, extra: list) -> str:
         n, gid = self.name, self.gid
         lines = [f"struct xgp_{n}_{gid}_{tag} {{", f"  struct xgh_{n}_{gid} h;",
@@ -879,9 +888,9 @@ class SweepGroupEmitter:
             if ox:
                 off.append(f"({ox})")
             idx = "c" + "".join(f" + {o}" for o in off)
-            return f"p.{b}[{idx}]"
+            return f"{b}[{idx}]"
         e = f"p.e{ld.slot}"
-        return (f"xg_ldc(p.{b}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, {e}[0], {e}[1], {e}[2]))")
+        return (f"xg_ldc({b}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, {e}[0], {e}[1], {e}[2]))")
 
     def value_code(self, sweep, fast: bool, indent: str) -> tuple[list, str]:
         """Preload lines and the value expression of a sweep at cell (z,y,x)=c."""
@@ -909,13 +918,13 @@ class SweepGroupEmitter:
             if any(s.store_offset):
                 oz, oy, ox = s.store_offset
                 e = f"p.e{s.slot}"
-                lines.append(f"{indent}  xg_stc(p.{dst}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, "
+                lines.append(f"{indent}  xg_stc({dst}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, "
                              f"{e}[0], {e}[1], {e}[2]), ({self.elem(s.slot)})({val}));")
             else:
-                lines.append(f"{indent}  p.{dst}[c] = {val};")
+                lines.append(f"{indent}  {dst}[c] = {val};")
             if s.implicit and not any(s.store_offset):
                 lines.append(f"{indent}}} else {{")
-                lines.append(f"{indent}  p.{dst}[c] = p.{src}[c];")
+                lines.append(f"{indent}  {dst}[c] = {src}[c];")
             lines.append(f"{indent}}}")
         return lines
 
@@ -932,8 +941,9 @@ class SweepGroupEmitter:
                 for a in range(3):
                     lo[a] = min(lo[a], ld.offset[a])
                     hi[a] = max(hi[a], ld.offset[a])
-        lines = [f"__global__ void __launch_bounds__(1024) xgk_{n}_{gid}_{tag}(const __grid_constant__ "
-                 f"struct xgp_{n}_{gid}_{tag} p) {{"] + TILE_PROLOGUE + [
+        lines = [f"template <typename I> __global__ void __launch_bounds__(256, 4) xgk_{n}_{gid}_{tag}("
+                 f"const __grid_constant__ struct xgp_{n}_{gid}_{tag} p) {{"] + TILE_PROLOGUE + \
+            self.restrict_locals([self.g.sweeps[j] for j in list(mains) + list(bnd_phases)]) + [
                  f"  const bool fast = p.same && z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && "
                  f"y0 + ({lo[1]}) >= 0 && y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;"]
         mask_vars = {}
@@ -963,7 +973,7 @@ class SweepGroupEmitter:
                       f"z = c / (p.e{s.slot}[2] * p.e{s.slot}[1]);",
                       "    (void)x; (void)y; (void)z;"]
             lines += pre
-            lines.append(f"    p.{dst}[c] = {val};")
+            lines.append(f"    {dst}[c] = {val};")
             lines += ["    }", "  }"]
         if final:
             lines += ["  __syncthreads();"] + CELL_LOOP
@@ -1026,7 +1036,8 @@ class SweepGroupEmitter:
         L += ["  dim3 block(tl[3], tl[4], tl[5]), grid;",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
               f"  xg_prof_launch({site}, s);",
-              f"  xgk_{n}_{gid}_{tag}<<<grid, block, 0, s>>>(p);",
+              f"  if (xg_small_index(p.Z, p.Y, p.X)) xgk_{n}_{gid}_{tag}<int><<<grid, block, 0, s>>>(p);",
+              f"  else xgk_{n}_{gid}_{tag}<int64_t><<<grid, block, 0, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
               f"  xg_prof_end({site}, s);"]
         if s.implicit:
@@ -1044,7 +1055,7 @@ class SweepGroupEmitter:
         dst = self.bname((s.slot, s.level, s.write_version))
         pre, val = self.value_code(s, False, "    ")
         K = [f"__global__ void __launch_bounds__(256) xgk_{n}_{gid}_{tag}(const __grid_constant__ "
-             f"struct xgp_{n}_{gid}_{tag} p) {{",
+             f"struct xgp_{n}_{gid}_{tag} p) {{"] + self.restrict_locals(sweeps) + [
              "  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < p.ncells; "
              "e += (int64_t)gridDim.x * blockDim.x) {",
              "    const int64_t c = p.cells[e];",
@@ -1055,10 +1066,10 @@ class SweepGroupEmitter:
         if any(s.store_offset):
             oz, oy, ox = s.store_offset
             e = f"p.e{s.slot}"
-            K.append(f"    xg_stc(p.{dst}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, {e}[0], {e}[1], {e}[2]), "
+            K.append(f"    xg_stc({dst}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, {e}[0], {e}[1], {e}[2]), "
                      f"({self.elem(s.slot)})({val}));")
         else:
-            K.append(f"    p.{dst}[c] = {val};")
+            K.append(f"    {dst}[c] = {val};")
         K += ["  }", "}"]
         self.gen.device_chunks.append("\n".join(K))
         L = [f"static int xgl_{n}_{gid}_{tag}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s) {{"]
@@ -1117,7 +1128,8 @@ class SweepGroupEmitter:
               "  dim3 block(tl[3], tl[4], tl[5]), grid;",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
               f"  xg_prof_launch({gid * 64 + 63 if swap else gid * 64 + 62}, s);",
-              f"  xgk_{n}_{gid}_{tag}<<<grid, block, 0, s>>>(p);",
+              f"  if (xg_small_index(p.Z, p.Y, p.X)) xgk_{n}_{gid}_{tag}<int><<<grid, block, 0, s>>>(p);",
+              f"  else xgk_{n}_{gid}_{tag}<int64_t><<<grid, block, 0, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
               f"  xg_prof_end({gid * 64 + 63 if swap else gid * 64 + 62}, s);"]
         for s in sweeps:

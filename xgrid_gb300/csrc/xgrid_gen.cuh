@@ -194,6 +194,10 @@ __device__ __forceinline__ xg_tile xg_tile_of(int64_t Z, int64_t Y, int64_t X, i
   return T;
 }
 
+// Tile kernels are instantiated for int and int64_t linear indices; the 32-bit
+// one (fewer integer instructions per load) runs when every index fits.
+static inline bool xg_small_index(int64_t Z, int64_t Y, int64_t X) { return Z * Y * X < (1LL << 31) - 1; }
+
 // Launch grid of a tiling; fails when an axis exceeds what CUDA allows.
 static inline int xg_tile_grid(int64_t ntx, int64_t nty, int64_t ntz, dim3* grid) {
   if (ntx > 2147483647LL || nty > 65535 || ntz > 65535) {

@@ -221,7 +221,7 @@ class MixedLoopEmitter:
         S = b.bname((slot, 0, 1))
         b.emit_fused(tag="res", extra_params=["float* mx_r", "float* mx_d"], extra_args=", float* mx_r, float* mx_d",
                      extra_fill=["  p.mx_r = mx_r; p.mx_d = mx_d;"],
-                     final=[f"const float rr = (float)(p.{S}[c] - p.{P0}[c]);", "p.mx_r[c] = rr;", "p.mx_d[c] = rr;"],
+                     final=[f"const float rr = (float)({S}[c] - {P0}[c]);", "p.mx_r[c] = rr;", "p.mx_d[c] = rr;"],
                      swap=False)
         defect = self.defect_kernel()
         cs = [f"struct xgm_{n}_{gid} {{"] + [f"  float {name};" for name, _, _ in self.coefs]
@@ -273,8 +273,8 @@ class MixedLoopEmitter:
                 oz, oy, ox = analysis.pad3(st.space_offset)
                 if fast:
                     off = "".join(f" + ({o}) * {s}" for o, s in ((oz, "sz"), (oy, "sy")) if o) + (f" + ({ox})" if ox else "")
-                    return f"p.{buf}[c{off}]"
-                return f"xg_ldc(p.{buf}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, p.Z, p.Y, p.X))"
+                    return f"{buf}[c{off}]"
+                return f"xg_ldc({buf}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, p.Z, p.Y, p.X))"
             return load
 
         def lin_code(sweep, buf, fast):
@@ -289,20 +289,23 @@ class MixedLoopEmitter:
         params.append("};")
         from .codegen import CELL_LOOP, TILE_PROLOGUE
         loop = CELL_LOOP
-        K = [f"__global__ void __launch_bounds__(1024) xgk_{n}_{gid}_mxd(const __grid_constant__ "
-             f"struct xgp_{n}_{gid}_mxd p) {{"] + TILE_PROLOGUE + [
+        K = [f"template <typename I> __global__ void __launch_bounds__(256, 6) xgk_{n}_{gid}_mxd("
+             f"const __grid_constant__ struct xgp_{n}_{gid}_mxd p) {{"] + TILE_PROLOGUE + [
              f"  const bool fast = z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && y0 + ({lo[1]}) >= 0 && "
              f"y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;",
              "  const bool mz = p.tzero0[t] != 0;",
+             "  const float* __restrict__ din = p.din;",
+             "  float* __restrict__ dout = p.dout;",
+             "  const float* __restrict__ rr = p.r;",
              "  if (fast && mz) {  // interior tile without boundary cells: one pass, r added directly"]
         K += ["  " + l for l in loop]
-        K += [f"      p.dout[c] = {lin_code(main, 'din', True)} + p.r[c];", "    }}", "    return;", "  }",
+        K += [f"      dout[c] = {lin_code(main, 'din', True)} + rr[c];", "    }}", "    return;", "  }",
               "  if (fast) {"]
         K += ["  " + l for l in loop]
-        K += [f"      p.dout[c] = (mz || p.m0[c] == 0) ? {lin_code(main, 'din', True)} : p.din[c];", "    }}",
+        K += [f"      dout[c] = (mz || p.m0[c] == 0) ? {lin_code(main, 'din', True)} : din[c];", "    }}",
               "  } else {"]
         K += ["  " + l for l in loop]
-        K += [f"      p.dout[c] = (mz || p.m0[c] == 0) ? {lin_code(main, 'din', False)} : p.din[c];", "    }}", "  }"]
+        K += [f"      dout[c] = (mz || p.m0[c] == 0) ? {lin_code(main, 'din', False)} : din[c];", "    }}", "  }"]
         for j in bnds:
             K += ["  __syncthreads();",
                   "  {",
@@ -312,10 +315,10 @@ class MixedLoopEmitter:
                   f"      const int64_t c = p.bc{j}[e];",
                   "      const int64_t x = c % p.X, y = (c / p.X) % p.Y, z = c / (p.X * p.Y);",
                   "      (void)x; (void)y; (void)z;",
-                  f"      p.dout[c] = {lin_code(sweeps[j], 'dout', False)};",
+                  f"      dout[c] = {lin_code(sweeps[j], 'dout', False)};",
                   "    }",
                   "  }"]
-        K += ["  __syncthreads();"] + loop + ["    p.dout[c] = p.dout[c] + p.r[c];", "  }}", "}"]
+        K += ["  __syncthreads();"] + loop + ["    dout[c] = dout[c] + rr[c];", "  }}", "}"]
         return ["\n".join(params), "\n".join(K)]
 
     def correction_kernel(self) -> list:
@@ -331,9 +334,10 @@ class MixedLoopEmitter:
         P = b.bname((slot, 0, 1))  # boundary phases address the target as version 1
         extra = ["const float* mx_d"] + [x for j in bnds for x in (f"const int32_t* bo{j}", f"const int64_t* bc{j}")]
         params = b.params_struct("mxc", bsweeps or [sweeps[0]], extra)
-        K = [f"__global__ void __launch_bounds__(1024) xgk_{n}_{gid}_mxc(const __grid_constant__ "
-             f"struct xgp_{n}_{gid}_mxc p) {{"] + TILE_PROLOGUE + CELL_LOOP + [
-             f"      p.{P}[c] = p.{P}[c] + (double)p.mx_d[c];", "    }}"]
+        K = [f"template <typename I> __global__ void __launch_bounds__(256, 6) xgk_{n}_{gid}_mxc("
+             f"const __grid_constant__ struct xgp_{n}_{gid}_mxc p) {{"] + TILE_PROLOGUE + b.restrict_locals(bsweeps or [sweeps[0]]) + \
+            ["  const float* __restrict__ mx_d = p.mx_d;"] + CELL_LOOP + [
+             f"      {P}[c] = {P}[c] + (double)mx_d[c];", "    }}"]
         for j in bnds:
             s = sweeps[j]
             pre, val = b.value_code(s, False, "    ")
@@ -345,7 +349,7 @@ class MixedLoopEmitter:
                   f"    const int64_t x = c % p.X, y = (c / p.X) % p.Y, z = c / (p.X * p.Y);",
                   "    (void)x; (void)y; (void)z;"]
             K += pre
-            K += [f"    p.{P}[c] = {val};", "    }", "  }"]
+            K += [f"    {P}[c] = {val};", "    }", "  }"]
         K.append("}")
         return [params, "\n".join(K)]
 
@@ -390,7 +394,8 @@ class MixedLoopEmitter:
         L += ["  dim3 block(tl[3], tl[4], tl[5]), grid;",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
               f"  xg_prof_launch({gid * 64 + 61}, s);",
-              f"  xgk_{n}_{gid}_mxd<<<grid, block, 0, s>>>(p);",
+              f"  if (xg_small_index(p.Z, p.Y, p.X)) xgk_{n}_{gid}_mxd<int><<<grid, block, 0, s>>>(p);",
+              f"  else xgk_{n}_{gid}_mxd<int64_t><<<grid, block, 0, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
               f"  xg_prof_end({gid * 64 + 61}, s);",
               "  return 0;", "}"]
@@ -411,7 +416,8 @@ class MixedLoopEmitter:
         L += ["  dim3 block(tl[3], tl[4], tl[5]), grid;",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
               f"  xg_prof_launch({gid * 64 + 60}, s);",
-              f"  xgk_{n}_{gid}_mxc<<<grid, block, 0, s>>>(p);",
+              f"  if (xg_small_index(p.Z, p.Y, p.X)) xgk_{n}_{gid}_mxc<int><<<grid, block, 0, s>>>(p);",
+              f"  else xgk_{n}_{gid}_mxc<int64_t><<<grid, block, 0, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
               f"  xg_prof_end({gid * 64 + 60}, s);",
               "  return 0;", "}"]
