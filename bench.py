@@ -65,8 +65,12 @@ def parse_args():
     ap.add_argument("--mixed-n", type=int, default=4097)
     ap.add_argument("--mixed-steps", type=int, default=500)
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--batch-steps", type=int, default=1000)
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--mixed", default=None, choices=[None, "fp32", "fp16", "bf16"],
                     help="kernels mode: precision lowering of the pressure loop")
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "batch"],
+                    help="kernels mode: which workload to run")
     ap.add_argument("--mode", default="bench", choices=["bench", "kernels"],
                     help="kernels: only run warm-up + steps (for profiler launch lists)")
     return ap.parse_args()
@@ -77,6 +81,15 @@ def kernels_only(args) -> None:
     import xgrid
     import workloads
     from xgrid_gb300 import device
+    if args.workload == "batch":
+        xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+                   opt_level=3, overstep="wrap")
+        probs = workloads.batch_setup(256, seed=1)
+        for _ in range(args.warmup + 1):
+            workloads.convdiff2d.batch(probs, args.steps)
+        device.synchronize()
+        print(json.dumps({"mode": "kernels", "workload": "batch", "calls": args.warmup + 1}))
+        return
     xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
                opt_level=3, mixed=args.mixed)
     grids, cfg = workloads.cavity_setup(args.n, stable_dt(args.n))
@@ -374,6 +387,57 @@ def mixed_section(n: int, steps: int) -> dict:
     return out
 
 
+def batch_section(count: int, steps: int, seq_steps: int) -> dict:
+    """256 periodic FP32 convection-diffusion problems of uneven size: one
+    persistent work-queue launch per step (graph over all steps) vs one call per
+    problem per step; GLUP/s and GB/s at 8 algorithmic bytes per update."""
+    import numpy as np
+    import torch
+
+    import xgrid
+    import workloads
+    from xgrid_gb300 import device
+    from xgrid_gb300.operator import Operator
+
+    xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+               opt_level=3, overstep="wrap")
+    k = Operator(workloads.convdiff2d.func, "kernel", "convdiff2d")
+    probs = workloads.batch_setup(count, seed=1)
+    cells = sum(int(np.prod(p[0].shape)) for p in probs)
+    s = device.stream()
+    k.batch(probs, steps)  # eager (descriptors, tables)
+    k.batch(probs, steps)  # capture
+    s.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    k.batch(probs, steps)
+    e1.record(s)
+    s.synchronize()
+    ms_b = e0.elapsed_time(e1)
+    for _ in range(2):
+        for args in probs:
+            k(*args)
+    s.synchronize()
+    e0.record(s)
+    for _ in range(seq_steps):
+        for args in probs:
+            k(*args)
+    e1.record(s)
+    s.synchronize()
+    ms_s = e0.elapsed_time(e1) * steps / seq_steps
+    hbm, src = peaks()
+    out = {"problems": count, "cells": cells, "steps": steps,
+           "batched": {"ms": ms_b, "value": cells * steps / (ms_b * 1e-3) / 1e9, "unit": "GLUP/s",
+                       "gbs": 8.0 * cells * steps / (ms_b * 1e-3) / 1e9},
+           "per_problem_calls": {"ms": ms_s, "value": cells * steps / (ms_s * 1e-3) / 1e9, "unit": "GLUP/s",
+                                 "timed_steps": seq_steps}}
+    out["batched"]["hbm_frac"] = out["batched"]["gbs"] / hbm
+    out["speedup_vs_per_problem"] = ms_s / ms_b
+    out["config"] = (f"{count} problems, extents U[64,1024] per axis (seed 1), FP32, periodic, convection-diffusion "
+                     f"5-point, {steps} steps in one CUDA graph of persistent launches")
+    return out
+
+
 def algorithmic_bytes(module, group: int) -> float:
     """Bytes per cell of one launch of ``group``: distinct buffers read (not
     produced earlier in the launch) plus distinct buffers written, main sweeps
@@ -441,6 +505,8 @@ def main():
     out = gpu_bench(args, rank, world)
     if rank == 0 and not args.no_mixed:
         out["mixed"] = mixed_section(args.mixed_n, args.mixed_steps)
+    if rank == 0 and not args.no_batch:
+        out["batched"] = batch_section(256, args.batch_steps, max(5, args.batch_steps // 50))
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)

@@ -131,3 +131,33 @@ def cavity_setup(n: int = 1025, dt: float = 1e-5):
         grids[k].boundary[...] = mask
     cfg = Config(1.0, 0.1, dt, 2.0 / (n - 1), 2.0 / (n - 1))
     return grids, cfg
+
+
+# ----------------------------------------------------------- batched problems
+@xgrid.kernel()
+def convdiff2d(u: float2d, a0: float, axm: float, axp: float, aym: float, ayp: float) -> None:
+    # linear convection-diffusion, central differences, written with coefficients
+    # only: a Python float literal is a C double, which would promote an FP32
+    # update to FP64 (periodic with overstep="wrap")
+    u[0, 0] = a0 * u[0, 0] + axm * u[0, -1] + axp * u[0, 1] + aym * u[-1, 0] + ayp * u[1, 0]
+
+
+def batch_setup(count: int = 256, seed: int = 1, lo: int = 64, hi: int = 1024):
+    """``count`` periodic FP32 problems: extents uniform in [lo, hi] per axis,
+    velocities c ~ U[-1, 1], nu ~ U[0.01, 0.1], u0 ~ U[0, 1), dt from the CFL and
+    diffusion limits; returns the argument tuples of ``convdiff2d``."""
+    rng = np.random.default_rng(seed)
+    problems = []
+    for _ in range(count):
+        ny, nx = (int(v) for v in rng.integers(lo, hi + 1, 2))
+        cx, cy = (float(v) for v in rng.uniform(-1.0, 1.0, 2))
+        nu = float(rng.uniform(0.01, 0.1))
+        dx, dy = 1.0 / nx, 1.0 / ny
+        dt = 0.2 * min(dx, dy) ** 2 / nu
+        u = xgrid.Grid((ny, nx), float)
+        u.now[...] = rng.random((ny, nx)).astype(u.numpy_dtype)
+        # per-step coefficients: central convection, explicit diffusion
+        gx, gy = 0.5 * cx * dt / dx, 0.5 * cy * dt / dy
+        kx, ky = nu * dt / (dx * dx), nu * dt / (dy * dy)
+        problems.append((u, 1.0 - 2.0 * kx - 2.0 * ky, gx + kx, kx - gx, gy + ky, ky - gy))
+    return problems

@@ -44,7 +44,7 @@ from .types import (Boolean, Floating, GridType, Ignore, Integer, Pointer, Struc
 OVERSTEP = {"none": "XG_OVERSTEP_NONE", "limit": "XG_OVERSTEP_LIMIT", "wrap": "XG_OVERSTEP_WRAP"}
 
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
-DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 32, 32, 32, 8, 1), 3: (1, 16, 32, 32, 8, 1)}
+DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 64, 32, 32, 8, 1), 3: (1, 16, 32, 32, 8, 1)}
 
 # tile prologue and cell loop shared by the tile kernels (32-bit coordinates,
 # 64-bit linear index per row)
@@ -125,6 +125,7 @@ class Module:
     return_type: object
     implicit_slots: list     # grid slots that need a scratch buffer
     aux_per_cell: dict       # grid slot -> bytes per cell of the mixed-precision work area
+    batch: bool              # the module exports the batched entry points
     groups: int
     device_only: bool        # kernel has no grid arguments (body runs on the device)
     sweeps: list             # analysis.Sweep per grid assignment (for the oracle and tests)
@@ -146,6 +147,7 @@ class CudaGenerator:
         self.group_tiling: dict = {}
         self.sweeps: list = []
         self.mixed_slots: dict = {}   # grid slot -> aux bytes per cell of mixed-precision loops
+        self.group_emitters: list = []
         self._plans: dict = {}
         self.slots = analysis.grid_slots(self.defn)
         self.grid_names = {name: i for name, i in self.slots.items()}
@@ -358,9 +360,11 @@ class CudaGenerator:
         self.sweeps.extend(sweeps)
         groups = analysis.build_groups(sweeps, self.group_counter, self.cfg.fuse)
         for g in groups:
-            dim = self.defn.signature.arguments[SweepGroupEmitter(self, g).arg_index(g.sweeps[0].slot)][1].dimension
+            em = SweepGroupEmitter(self, g)
+            dim = self.defn.signature.arguments[em.arg_index(g.sweeps[0].slot)][1].dimension
             self.group_tiling[g.index] = DEFAULT_TILING[dim]
-            SweepGroupEmitter(self, g).emit(env, indent, out)
+            em.emit(env, indent, out)
+            self.group_emitters.append(em)
 
     # ================================================================ module
     def generate(self) -> Module:
@@ -420,9 +424,18 @@ class CudaGenerator:
         for gi in range(max(self.group_counter[0], 1)):
             src.append("  {" + ", ".join(str(v) for v in self.group_tiling.get(gi, DEFAULT_TILING[2])) + "},")
         src.append("};")
+        batch_host = None
+        from . import batch as batch_mod
+        if (not device_only and batch_mod.qualifies(self) and len(self.group_emitters) == 1
+                and batch_mod.BatchEmitter.usable(self.group_emitters[0].g)):
+            em = self.group_emitters[0]
+            dev, batch_host = batch_mod.BatchEmitter(self, em.g, em).emit(value_args)
+            self.device_chunks.extend(dev)
         src.extend(self.device_chunks)
         src.extend(self.host_chunks)
         src.extend(body)
+        if batch_host:
+            src.append(batch_host)
         src.append(f'extern "C" int xg_config_{name}(int group, const int32_t* cfg, int fuse) {{')
         src.append(f"  if (fuse >= 0) xg_fuse_{name} = fuse;")
         src.append(f"  if (group < 0 || group >= {self.group_counter[0]} || !cfg) return 0;")
@@ -430,12 +443,18 @@ class CudaGenerator:
         src.append("  return 0;")
         src.append("}")
         src.append(f'extern "C" int xg_groups_{name}(void) {{ return {self.group_counter[0]}; }}')
+        src.append(f'extern "C" int xg_get_tiling_{name}(int group, int32_t* cfg) {{')
+        src.append(f"  if (group < 0 || group >= {max(self.group_counter[0], 1)}) return -1;")
+        src.append(f"  for (int i = 0; i < 6; ++i) cfg[i] = xg_tiling_{name}[group][i];")
+        src.append("  return 0;")
+        src.append("}")
         src.append(f'extern "C" int xg_mixed_{name}(int64_t every) {{ xg_mixed_every_{name} = every; return 0; }}')
         implicit = sorted({s.slot for s in self.sweeps if s.implicit})
         if getattr(self.op, "noalloc", False) and grid_args and implicit:
             src.extend(self.noalloc_entry(name, entry, grid_args, implicit))
         return Module("\n".join(src) + "\n", name, entry, self.depth + 1, grid_args, value_args, order, rtype,
-                      implicit, dict(self.mixed_slots), self.group_counter[0], device_only, self.sweeps)
+                      implicit, dict(self.mixed_slots), batch_host is not None, self.group_counter[0], device_only,
+                      self.sweeps)
 
     def noalloc_entry(self, name, entry, grid_args, implicit) -> list[str]:
         """``<entry>_noalloc``: same computation as ``<entry>``, for callers that
@@ -856,6 +875,13 @@ class SweepGroupEmitter:
                 out.append(b[0])
         return out
 
+    def min_blocks(self) -> int:
+        """Resident 256-thread CTAs per SM asked of ptxas: FP64 sweeps are bound by
+        the FP64 pipe and keep registers for ILP; FP32/integer sweeps are memory
+        bound and want occupancy."""
+        wide = any(self.elem(b[0]) == "double" for b in self.buffers(self.g.sweeps))
+        return 4 if wide else 6
+
     def restrict_locals(self, sweeps) -> list:
         """Kernel-local __restrict__ copies of the buffer pointers: distinct buffer
         names never alias (a grid is passed once; levels and scratch are separate
@@ -876,9 +902,36 @@ class SweepGroupEmitter:
         lines.append("};")
         return "\n".join(lines)
 
-    def load_code(self, sweep, ld: analysis.Load, fast: bool) -> str:
+    @staticmethod
+    def axis_name(axis: str, o: int) -> str:
+        return axis if o == 0 else f"w{axis}_{'m' if o < 0 else 'p'}{abs(o)}"
+
+    def axis_decls(self, sweeps, indent: str) -> list:
+        """Edge-tile coordinates (wrap/limit) for every axis offset the loads use."""
+        if self.gen.cfg.overstep == "none":
+            return []
+        used = set()
+        for s in sweeps:
+            for _, ld in s.loads:
+                for axis, o in zip("zyx", ld.offset):
+                    if o:
+                        used.add((axis, o))
+        ext = {"z": "p.Z", "y": "p.Y", "x": "p.X"}
+        return [f"{indent}const int {self.axis_name(a, o)} = xg_axis(xg_overstep, {a} + ({o}), (int){ext[a]});"
+                for a, o in sorted(used)]
+
+    def load_code(self, sweep, ld: analysis.Load, fast) -> str:
+        """Load of one stencil: ``fast`` (True) unchecked interior addressing,
+        "edge" per-axis edge coordinates (all grids of the domain's extent),
+        False generic per-grid addressing."""
         b = self.bname((ld.slot, ld.level, ld.version))
         oz, oy, ox = ld.offset
+        if fast == "edge":
+            if self.gen.cfg.overstep == "none":
+                off = f"({oz}) * (int64_t)sz + ({oy}) * (int64_t)sy + ({ox})"
+                return f"xg_ldc({b}, xg_flat((int64_t)c + {off}, (int64_t)sz * p.Z))"
+            return (f"{b}[(I){self.axis_name('z', oz)} * sz + (I){self.axis_name('y', oy)} * sy + "
+                    f"(I){self.axis_name('x', ox)}]")
         if fast:
             off = []
             if oz:
@@ -905,8 +958,10 @@ class SweepGroupEmitter:
         env = SweepEnv(self.gen, self.hoist_map, names, self.div_map)
         return lines, self.gen.expr(sweep.stmt.value, env)
 
-    def main_body(self, sweeps_idx: list, fast: bool, indent: str, mask_vars: dict) -> list:
+    def main_body(self, sweeps_idx: list, fast, indent: str, mask_vars: dict) -> list:
         lines = []
+        if fast == "edge":
+            lines += self.axis_decls([self.g.sweeps[j] for j in sweeps_idx], indent)
         for j in sweeps_idx:
             s = self.g.sweeps[j]
             dst = self.bname((s.slot, s.level, s.write_version))
@@ -941,7 +996,7 @@ class SweepGroupEmitter:
                 for a in range(3):
                     lo[a] = min(lo[a], ld.offset[a])
                     hi[a] = max(hi[a], ld.offset[a])
-        lines = [f"template <typename I> __global__ void __launch_bounds__(256, 4) xgk_{n}_{gid}_{tag}("
+        lines = [f"template <typename I> __global__ void __launch_bounds__(256, {self.min_blocks()}) xgk_{n}_{gid}_{tag}("
                  f"const __grid_constant__ struct xgp_{n}_{gid}_{tag} p) {{"] + TILE_PROLOGUE + \
             self.restrict_locals([self.g.sweeps[j] for j in list(mains) + list(bnd_phases)]) + [
                  f"  const bool fast = p.same && z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && "
@@ -953,6 +1008,10 @@ class SweepGroupEmitter:
         lines.append("  if (fast) {")
         lines += ["  " + l for l in CELL_LOOP]
         lines += self.main_body(mains, True, "      ", mask_vars)
+        lines.append("    }}")
+        lines.append("  } else if (p.same) {")
+        lines += ["  " + l for l in CELL_LOOP]
+        lines += self.main_body(mains, "edge", "      ", mask_vars)
         lines.append("    }}")
         lines.append("  } else {")
         lines += ["  " + l for l in CELL_LOOP]

@@ -129,6 +129,19 @@ static inline bool xg_same_ext(xg_ext a, xg_ext b) { return a.z == b.z && a.y ==
 //   wrap : periodic per axis            (xgrid/lang/generator.py:172-173)
 //   limit: clamped per axis              (xgrid/lang/generator.py:174-175)
 //   none : row-major flattened offset    (xgrid/lang/generator.py:176-179)
+// Periodic index: one compare-and-add for offsets up to one period (the
+// stencil case), a remainder only beyond that.
+__device__ __forceinline__ int64_t xg_wrap(int64_t c, int64_t n) {
+  if (c < 0) {
+    c += n;
+    if (c < 0) c = ((c % n) + n) % n;
+  } else if (c >= n) {
+    c -= n;
+    if (c >= n) c %= n;
+  }
+  return c;
+}
+
 __device__ __forceinline__ int64_t xg_addr(int mode, int64_t z, int64_t y, int64_t x, int oz, int oy, int ox,
                                            int64_t Z, int64_t Y, int64_t X) {
   if (mode == XG_OVERSTEP_NONE) {
@@ -137,9 +150,9 @@ __device__ __forceinline__ int64_t xg_addr(int mode, int64_t z, int64_t y, int64
   }
   int64_t cz = z + oz, cy = y + oy, cx = x + ox;
   if (mode == XG_OVERSTEP_WRAP) {
-    cz = ((cz % Z) + Z) % Z;
-    cy = ((cy % Y) + Y) % Y;
-    cx = ((cx % X) + X) % X;
+    cz = xg_wrap(cz, Z);
+    cy = xg_wrap(cy, Y);
+    cx = xg_wrap(cx, X);
   } else {
     cz = cz < 0 ? 0 : (cz >= Z ? Z - 1 : cz);
     cy = cy < 0 ? 0 : (cy >= Y ? Y - 1 : cy);
@@ -147,6 +160,25 @@ __device__ __forceinline__ int64_t xg_addr(int mode, int64_t z, int64_t y, int64
   }
   return (cz * Y + cy) * X + cx;
 }
+
+// One coordinate of an edge tile under wrap or limit (the same rules as
+// xg_addr, computed once per cell and axis offset instead of once per load).
+__device__ __forceinline__ int xg_axis(int mode, int c, int n) {
+  if (mode == XG_OVERSTEP_WRAP) {
+    if (c < 0) {
+      c += n;
+      if (c < 0) c = ((c % n) + n) % n;
+    } else if (c >= n) {
+      c -= n;
+      if (c >= n) c %= n;
+    }
+    return c;
+  }
+  return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
+// Flattened neighbour under "none": -1 outside the allocation.
+__device__ __forceinline__ int64_t xg_flat(int64_t t, int64_t total) { return (t < 0 || t >= total) ? -1 : t; }
 
 template <typename T>
 __device__ __forceinline__ T xg_ldc(const T* p, int64_t i) {

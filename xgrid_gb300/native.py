@@ -66,7 +66,8 @@ class NativeKernel:
         runtime.load().xg_graph_clear(self.fn_ptr)
 
     # ------------------------------------------------------------------ call
-    def __call__(self, *args):
+    def split(self, args):
+        """(grids, values) of one call's arguments, type-checked."""
         if len(args) != self.nargs:
             raise TypeError(f"this function takes {self.nargs} argument ({len(args)} given)")
         grids, values = [], []
@@ -81,6 +82,10 @@ class NativeKernel:
                 grids.append(a)
             else:
                 values.append(a)
+        return grids, values
+
+    def __call__(self, *args):
+        grids, values = self.split(args)
         if len({id(g) for g in grids}) != len(grids):
             self.logger.dead("the same Grid is passed twice to one kernel call")
         device.require_cuda()
@@ -117,3 +122,101 @@ class NativeKernel:
         for (name, t), v in zip(self.module.value_args, values):
             setattr(packed, name, t.serialize(v))
         return packed
+
+    # --------------------------------------------------------------- batched
+    def batch(self, problems, steps: int = 1) -> None:
+        """Batched execution (see ``xgrid_gb300.batch``)."""
+        if not self.module.batch:
+            self.logger.dead(f"kernel '{self.module.name}' cannot run batched: its body must be one run of "
+                             f"explicit mask-0 grid assignments")
+        steps = int(steps)
+        if steps <= 0 or not problems:
+            return
+        device.require_cuda()
+        lib = self.lib.dylib
+        if not hasattr(self, "_batch"):
+            info = getattr(lib, f"xg_batch_info_{self.module.name}")
+            depth, dsize, group = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+            info(ctypes.byref(depth), ctypes.byref(dsize), ctypes.byref(group))
+            prep = getattr(lib, f"xg_batch_prepare_{self.module.name}")
+            prep.restype = ctypes.c_int
+            blocks_fn = getattr(lib, f"xg_batch_blocks_{self.module.name}")
+            blocks_fn.restype = ctypes.c_int
+            fn = getattr(lib, f"xg_batch_{self.module.name}")
+            self._batch = {"depth": depth.value, "dsize": dsize.value, "group": group.value, "prep": prep,
+                           "blocks": blocks_fn, "fn": ctypes.cast(fn, ctypes.c_void_p).value, "desc": {},
+                           "counters": None, "nblocks": {}}
+        B = self._batch
+        all_grids, all_values = [], []
+        for args in problems:
+            grids, values = self.split(tuple(args))
+            all_grids.extend(grids)
+            all_values.append(values)
+        if len({id(g) for g in all_grids}) != len(all_grids):
+            self.logger.dead("batched problems must not share grids")
+        uploaded = False
+        for g in all_grids:
+            g._extend_time(B["depth"])
+            uploaded |= g._sync_device(False)
+        if uploaded:
+            device.stream().synchronize()
+        nprob = len(problems)
+        ng = len(self.module.grid_args)
+        arr = (runtime.XGGrid * (nprob * ng))(*[g.serialize() for g in all_grids])
+        packed = b"".join(bytes(self.pack(v)) for v in all_values)
+        stride = ctypes.sizeof(self.args_type) if self.module.value_args else 0
+        tiling = self._tiling_key(B["group"])
+        key = (tuple((st.level[k] or 0) for st in arr for k in range(B["depth"])),
+               tuple(st.mask or 0 for st in arr), tuple(runtime.load().xg_mask_version(st.mask) for st in arr),
+               packed, tiling)
+        entry = B["desc"].get(key)
+        if entry is None:
+            host = ctypes.create_string_buffer(nprob * (B["dsize"] + 8))
+            total, maxc = ctypes.c_int64(), ctypes.c_int64()
+            args_buf = ctypes.create_string_buffer(packed, max(len(packed), 1))
+            rc = B["prep"](arr, ctypes.c_int(nprob), args_buf, ctypes.c_size_t(stride), host,
+                           ctypes.c_size_t(len(host)), ctypes.byref(total), ctypes.byref(maxc))
+            if rc != 0:
+                self.logger.dead(f"batch preparation failed: {runtime.last_error()}")
+            t = device.torch()
+            dev = device.alloc_bytes(len(host))
+            with t.cuda.stream(device.stream()):
+                dev[: len(host)].copy_(t.frombuffer(bytearray(host.raw), dtype=t.uint8), non_blocking=False)
+            if len(B["desc"]) > 16:
+                B["desc"].clear()
+            entry = B["desc"][key] = (dev, total.value, maxc.value)
+        dev, total, maxc = entry
+        if B["counters"] is None or B["counters"].numel() < steps * 8:
+            B["counters"] = device.alloc_bytes(steps * 8)
+        block = tiling[3:6]
+        threads = block[0] * block[1] * block[2]
+        if threads not in B["nblocks"]:
+            nb = ctypes.c_int()
+            if B["blocks"](ctypes.c_int(threads), ctypes.byref(nb)) != 0:
+                self.logger.dead(runtime.last_error())
+            B["nblocks"][threads] = nb.value
+        ba = BatchArgs(dev.data_ptr(), total, steps, 0, B["counters"].data_ptr(), nprob, 1 if self.op.tick else 0,
+                       1 if maxc < (1 << 31) - 1 else 0, B["nblocks"][threads], (ctypes.c_int32 * 3)(*block))
+        rc = runtime.load().xg_call(B["fn"], None, 0, ctypes.cast(ctypes.byref(ba), ctypes.c_void_p),
+                                    ctypes.sizeof(ba), None, 0, device.stream_handle(), 1 if self.use_graph else 0)
+        if rc != 0:
+            self.logger.dead(f"batched kernel '{self.module.name}' failed: {runtime.last_error()}")
+        for g in all_grids:
+            if self.op.tick:
+                for _ in range(steps % B["depth"]):
+                    g._levels.insert(0, g._levels.pop())
+            for lv in g._levels:
+                lv.auth = "dev"
+
+    def _tiling_key(self, group: int) -> tuple:
+        arr = (ctypes.c_int32 * 6)()
+        getter = getattr(self.lib.dylib, f"xg_get_tiling_{self.module.name}")
+        getter(ctypes.c_int(group), arr)
+        return tuple(arr)
+
+
+class BatchArgs(ctypes.Structure):
+    _fields_ = [("desc", ctypes.c_void_p), ("total", ctypes.c_int64), ("steps", ctypes.c_int64),
+                ("step0", ctypes.c_int64), ("counters", ctypes.c_void_p), ("nprob", ctypes.c_int32),
+                ("tick", ctypes.c_int32), ("small", ctypes.c_int32), ("blocks", ctypes.c_int32),
+                ("block", ctypes.c_int32 * 3)]

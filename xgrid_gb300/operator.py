@@ -44,6 +44,16 @@ class Operator:
             return self.func(*args)
         self.logger.dead(f"Invalid call to non-kernel or non-function ({self.mode}) operator '{self.name}'")
 
+    def batch(self, problems, steps: int = 1) -> None:
+        """Run ``steps`` calls of this kernel on each of ``problems`` (argument
+        tuples of independent problems) with one persistent launch per step."""
+        if self.mode != "kernel":
+            self.logger.dead(f"Only kernels can be batched, '{self.name}' is a {self.mode}")
+        if self.native is None:
+            from .native import NativeKernel
+            self.native = NativeKernel(self)
+        return self.native.batch(problems, steps)
+
     @property
     def ir(self) -> ir.Definition:
         cached = getattr(self, "_ir", None)
