@@ -161,3 +161,27 @@ def batch_setup(count: int = 256, seed: int = 1, lo: int = 64, hi: int = 1024):
         kx, ky = nu * dt / (dx * dx), nu * dt / (dy * dy)
         problems.append((u, 1.0 - 2.0 * kx - 2.0 * ky, gx + kx, kx - gx, gy + ky, ky - gy))
     return problems
+
+
+# ------------------------------------------------------------- differentiation
+@xgrid.kernel()
+def diffuse3d(u: float3d, k: float3d, dt: float) -> None:
+    # variable-coefficient 7-point diffusion; face diffusivity (k_c + k_nb) / 2 with
+    # the 1/2 and 1/h^2 folded into dt (periodic with overstep="wrap")
+    u[0, 0, 0] = u[0, 0, 0] + dt * ((k[0, 0, 0] + k[1, 0, 0]) * (u[1, 0, 0] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[-1, 0, 0]) * (u[-1, 0, 0] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[0, 1, 0]) * (u[0, 1, 0] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[0, -1, 0]) * (u[0, -1, 0] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[0, 0, 1]) * (u[0, 0, 1] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[0, 0, -1]) * (u[0, 0, -1] - u[0, 0, 0]))
+
+
+def adjoint_setup(n: int = 256, seed: int = 2):
+    """u0 ~ U[0,1), kappa log-uniform in [0.01, 0.1], target ~ U[0,1) (seeded);
+    dt at 0.8 of the explicit stability limit for kappa_max = 0.1."""
+    rng = np.random.default_rng(seed)
+    u0 = rng.random((n, n, n), dtype=np.float32)
+    kappa = np.exp(rng.uniform(np.log(0.01), np.log(0.1), (n, n, n))).astype(np.float32)
+    target = rng.random((n, n, n), dtype=np.float32)
+    dt = 0.8 / (12.0 * 0.1)
+    return u0, kappa, target, dt

@@ -1,0 +1,501 @@
+"""Adjoint (reverse-mode) kernels generated from a stencil kernel's DSL body.
+
+For a kernel whose body is one explicit sweep of the target ``u``::
+
+    u'(c) = f( u(c + o_1), ..., u(c + o_m), k(c + q_1), ..., scalars )
+
+(loads of ``u`` from the previous level, coefficient grids ``k`` that the kernel
+never writes), one step's vector-Jacobian product in gather form is::
+
+    lam(x)  =      sum_i  lam'(x - o_i) * df/du_i |(x - o_i)
+    g_k(x) +=      sum_j  lam'(x - q_j) * df/dk_j |(x - q_j)
+
+where ``df/dL |(c)`` is the symbolic partial derivative of the right-hand side
+with respect to load ``L``, evaluated with every load shifted to cell ``c`` —
+the forward offsets transposed.  The partials are derived here from the IR
+(sum, product and quotient rules, integer powers), the result is emitted as a
+CUDA tile kernel in the kernel's arithmetic type, and
+``rollout(...)`` wraps forward steps and adjoint steps in a
+``torch.autograd.Function`` with checkpoints every ``checkpoint_every`` steps
+and recomputation of each segment during the backward pass.
+
+Every cell must be updated each step (all-zero masks), so that the step is a
+function of the previous state only.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import hashlib
+
+from . import analysis, ir
+from .log import Logger
+from .types import Floating, GridType
+
+B = ir.BinaryOperator
+LOG = Logger("xgrid.adjoint")
+
+
+# ------------------------------------------------------------ symbolic algebra
+# nodes: ("c", float) | ("p", name) | ("l", (slot, level, offset)) | (op, a, b) | ("neg", a)
+ZERO, ONE = ("c", 0.0), ("c", 1.0)
+
+
+def s_add(a, b):
+    if a == ZERO:
+        return b
+    if b == ZERO:
+        return a
+    return ("+", a, b)
+
+
+def s_sub(a, b):
+    if b == ZERO:
+        return a
+    if a == ZERO:
+        return s_neg(b)
+    return ("-", a, b)
+
+
+def s_mul(a, b):
+    if a == ZERO or b == ZERO:
+        return ZERO
+    if a == ONE:
+        return b
+    if b == ONE:
+        return a
+    return ("*", a, b)
+
+
+def s_div(a, b):
+    if a == ZERO:
+        return ZERO
+    if b == ONE:
+        return a
+    return ("/", a, b)
+
+
+def s_neg(a):
+    if a == ZERO:
+        return ZERO
+    if a[0] == "neg":
+        return a[1]
+    return ("neg", a)
+
+
+def diff(node, wrt):
+    kind = node[0]
+    if kind in ("c", "p"):
+        return ZERO
+    if kind == "l":
+        return ONE if node[1] == wrt else ZERO
+    if kind == "neg":
+        return s_neg(diff(node[1], wrt))
+    a, b = node[1], node[2]
+    da, db = diff(a, wrt), diff(b, wrt)
+    if kind == "+":
+        return s_add(da, db)
+    if kind == "-":
+        return s_sub(da, db)
+    if kind == "*":
+        return s_add(s_mul(da, b), s_mul(a, db))
+    if kind == "/":
+        return s_sub(s_div(da, b), s_div(s_mul(a, db), s_mul(b, b)))
+    raise ValueError(kind)
+
+
+def loads_of(node, out=None):
+    out = [] if out is None else out
+    if node[0] == "l":
+        if node[1] not in out:
+            out.append(node[1])
+    elif node[0] in ("+", "-", "*", "/"):
+        loads_of(node[1], out)
+        loads_of(node[2], out)
+    elif node[0] == "neg":
+        loads_of(node[1], out)
+    return out
+
+
+def shift(node, d):
+    """Every load moved by -d (evaluation at cell x - d)."""
+    if node[0] == "l":
+        slot, level, off = node[1]
+        return ("l", (slot, level, tuple(o - s for o, s in zip(off, d))))
+    if node[0] in ("+", "-", "*", "/"):
+        return (node[0], shift(node[1], d), shift(node[2], d))
+    if node[0] == "neg":
+        return ("neg", shift(node[1], d))
+    return node
+
+
+class AdjointGenerator:
+    """Builds the adjoint CUDA module of one kernel."""
+
+    def __init__(self, gen) -> None:
+        from .codegen import SweepGroupEmitter
+        self.gen = gen
+        d = gen.defn
+        body = d.body
+        if len(body) != 1 or not isinstance(body[0], ir.Assignment) or not isinstance(body[0].terminal, ir.Stencil):
+            LOG.dead(f"kernel '{gen.op.name}': the adjoint needs a body of exactly one grid assignment")
+        st = body[0].terminal
+        if st.boundary_mask != 0 or any(st.space_offset) or st.time_offset != 0:
+            LOG.dead("the adjoint needs a mask-0 assignment to time 0 at offset 0")
+        self.stmt = body[0]
+        self.target = st.variable.name
+        self.slot = gen.slots[self.target]
+        ttype = d.scope[self.target].type
+        if not isinstance(ttype.element, Floating):
+            LOG.dead("the adjoint needs a floating-point grid")
+        self.T = "double" if ttype.element.width_bytes == 8 else "float"
+        sweep = analysis.collect_sweep(self.stmt, gen.slots, gen.logger)
+        if sweep.implicit:
+            LOG.dead("the adjoint does not support in-place (time-0) reads of the target")
+        groups = analysis.build_groups([sweep], [0], True)
+        self.group = groups[0]
+        self.em = SweepGroupEmitter(gen, self.group)
+        self.em.prepare()
+        self.params: dict = {}
+        self.expr = self.to_sym(self.stmt.value)
+        self.loads = loads_of(self.expr)
+        for slot, level, _ in self.loads:
+            if slot == self.slot and level == 0:
+                LOG.dead("the adjoint needs the target read from the previous level only")
+
+    # IR → algebra (hoisted launch constants become parameters)
+    def to_sym(self, e):
+        h = self.em.hoist_map.get(id(e))
+        if h is not None:
+            self.params[h.name] = h
+            return ("p", h.name)
+        if isinstance(e, ir.Constant):
+            return ("c", float(e.value))
+        if isinstance(e, ir.Stencil):
+            return ("l", (self.gen.slots[e.variable.name], abs(e.time_offset), analysis.pad3(e.space_offset)))
+        if isinstance(e, ir.Unary):
+            a = self.to_sym(e.right)
+            return s_neg(a) if e.operator is ir.UnaryOperator.Neg else a
+        if isinstance(e, ir.Cast):
+            return self.to_sym(e.value)
+        if isinstance(e, ir.Binary):
+            div = self.em.div_map.get(id(e))
+            if div is not None:  # division by a launch constant: its value is the divisor's d
+                return s_div(self.to_sym(e.left), ("p", div.name + ".d"))
+            a, b = self.to_sym(e.left), self.to_sym(e.right)
+            if e.operator is B.Add:
+                return s_add(a, b)
+            if e.operator is B.Sub:
+                return s_sub(a, b)
+            if e.operator is B.Mul:
+                return s_mul(a, b)
+            if e.operator is B.Div:
+                return s_div(a, b)
+            if e.operator is B.Pow and isinstance(e.right, ir.Constant) and float(e.right.value) == 2.0:
+                return s_mul(a, a)
+        LOG.dead(f"the adjoint cannot differentiate '{type(e).__name__}' expressions")
+
+    def emit_sym(self, node, loadname) -> str:
+        T = self.T
+        k = node[0]
+        if k == "c":
+            return f"(({T}){node[1]!r})"
+        if k == "p":
+            return f"(({T})p.h.{node[1]})"
+        if k == "l":
+            return loadname(node[1])
+        if k == "neg":
+            return f"(-{self.emit_sym(node[1], loadname)})"
+        return f"({self.emit_sym(node[1], loadname)} {k} {self.emit_sym(node[2], loadname)})"
+
+    def source(self) -> tuple[str, str]:
+        """(CUDA source, entry symbol)."""
+        from .codegen import c_type
+        gen, em = self.gen, self.em
+        n = gen.op.name
+        T = self.T
+        slots_used = sorted({ld[0] for ld in self.loads} | {self.slot})
+        # adjoint terms: for every load L of the forward expression, with offset o:
+        #   contribution to grad(grid of L)(x) = lam'(x - o) * (df/dL)(x - o)
+        terms = {}
+        for key in self.loads:
+            slot, level, off = key
+            d = diff(self.expr, key)
+            if d == ZERO:
+                continue
+            terms.setdefault(slot, []).append((off, shift(d, off)))
+        loads_needed = []
+        for slot, lst in terms.items():
+            for off, d in lst:
+                for ld in loads_of(d):
+                    if ld not in loads_needed:
+                        loads_needed.append(ld)
+        lam_offsets = sorted({tuple(-o for o in off) for lst in terms.values() for off, _ in lst})
+        names = {}
+
+        def loadname(key):
+            return names[key]
+
+        def addr(off):
+            oz, oy, ox = off
+            return f"xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, p.Z, p.Y, p.X)"
+
+        lines = [f"struct xgadj_{n} {{", f"  struct xgh_{n}_{self.group.index} h;", "  int64_t Z, Y, X;",
+                 "  int32_t tz, ty, tx;", "  int64_t ntz, nty, ntx;",
+                 f"  const {T}* lam_in;", f"  {T}* lam_out;"]
+        for slot in slots_used:
+            lines.append(f"  const {T}* f{slot}[{gen.depth + 1}];")
+            lines.append(f"  {T}* g{slot};")
+        lines.append("};")
+        allofs = [tuple(o for o in off) for off in lam_offsets] + [k[2] for k in loads_needed]
+        lo = [min([0] + [o[a_] for o in allofs]) for a_ in range(3)]
+        hi = [max([0] + [o[a_] for o in allofs]) for a_ in range(3)]
+        from .codegen import CELL_LOOP, TILE_PROLOGUE
+
+        def body(fast):
+            out = []
+            def ld(buf, off):
+                if fast:
+                    oz, oy, ox = off
+                    return f"{buf}[c + ({oz}) * sz + ({oy}) * sy + ({ox})]"
+                return f"xg_ldc({buf}, {addr(off)})"
+            for i, off in enumerate(lam_offsets):
+                names[("lam", off)] = f"a{i}"
+                out.append(f"      const {T} a{i} = {ld('p.lam_in', off)};")
+            for i, key in enumerate(loads_needed):
+                slot, level, off = key
+                names[key] = f"v{i}"
+                out.append(f"      const {T} v{i} = {ld(f'p.f{slot}[{level}]', off)};")
+            for slot in slots_used:
+                acc = []
+                for off, d in terms.get(slot, []):
+                    lam = names[("lam", tuple(-o for o in off))]
+                    acc.append(f"({lam} * {self.emit_sym(d, loadname)})")
+                total = " + ".join(acc) if acc else f"(({T})0)"
+                if slot == self.slot:
+                    out.append(f"      p.lam_out[c] = {total};")
+                else:
+                    out.append(f"      if (p.g{slot}) p.g{slot}[c] = p.g{slot}[c] + ({total});")
+            return out
+
+        K = [f"template <typename I> __global__ void __launch_bounds__(256) xgk_{n}_adjoint("
+             f"const __grid_constant__ struct xgadj_{n} p) {{"] + TILE_PROLOGUE + [
+             f"  const bool fast = z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && y0 + ({lo[1]}) >= 0 && "
+             f"y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;",
+             "  if (fast) {"]
+        K += ["  " + l for l in CELL_LOOP] + body(True) + ["    }}", "  } else {"]
+        K += ["  " + l for l in CELL_LOOP] + body(False) + ["    }}", "  }", "}"]
+        ns = len(gen.slots)
+        value_args = [(a, t) for a, t in gen.defn.signature.arguments if not isinstance(t, GridType)]
+        H = [f'extern "C" int xg_adjoint_{n}(void* lam_out, const void* lam_in, const void* const* fields, '
+             f'void* const* grads, const int64_t* shape, const void* args, size_t nargs, void* stream) {{',
+             "  cudaStream_t s = (cudaStream_t)stream;",
+             f"  struct xga_{n} a;",
+             "  memset(&a, 0, sizeof a);",
+             "  if (nargs) memcpy(&a, args, nargs < sizeof a ? nargs : sizeof a);"]
+        for an, at in value_args:
+            H.append(f"  {c_type(at)} {an} = a.{an}; (void){an};")
+        from .codegen import HostEnv
+        H += em.host_hoists(HostEnv(gen), "  ")
+        H += [f"  struct xgadj_{n} p;", "  memset(&p, 0, sizeof p);", "  p.h = h_;",
+              "  p.Z = shape[0]; p.Y = shape[1]; p.X = shape[2];",
+              f"  p.lam_in = (const {T}*)lam_in; p.lam_out = ({T}*)lam_out;"]
+        for slot in slots_used:
+            for lv in range(gen.depth + 1):
+                H.append(f"  p.f{slot}[{lv}] = (const {T}*)fields[{slot} * {gen.depth + 1} + {lv}];")
+            H.append(f"  p.g{slot} = ({T}*)grads[{slot}];")
+        H += ["  p.tz = 1; p.ty = 8; p.tx = 32;",
+              "  p.ntz = xg_tiles_along(p.Z, p.tz); p.nty = xg_tiles_along(p.Y, p.ty); p.ntx = xg_tiles_along(p.X, p.tx);",
+              "  dim3 grid, block(32, 8, 1);",
+              "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
+              "  xg_prof_launch(-2, s);",
+              f"  if (xg_small_index(p.Z, p.Y, p.X)) xgk_{n}_adjoint<int><<<grid, block, 0, s>>>(p);",
+              f"  else xgk_{n}_adjoint<int64_t><<<grid, block, 0, s>>>(p);",
+              "  XG_CUDA(cudaGetLastError());",
+              "  xg_prof_end(-2, s);",
+              "  return 0;", "}"]
+        # the module also needs the hoisted-value struct and the argument struct
+        hs = [f"struct xgh_{n}_{self.group.index} {{"] + [f"  {h.ctype} {h.name};" for h in em.hoisted]
+        if not em.hoisted:
+            hs.append("  char xg_empty;")
+        hs.append("};")
+        ga = [f"struct xga_{n} {{"] + [f"  {c_type(t)} {an};" for an, t in value_args]
+        if not value_args:
+            ga.append("  char xg_empty;")
+        ga.append("};")
+        structs = gen.struct_defs()
+        src = ['#include "xgrid_gen.cuh"', f"static const int xg_overstep = {gen.mode};"] + structs + ga + hs + \
+            lines + K + H
+        return "\n".join(src) + "\n", f"xg_adjoint_{n}"
+
+
+def build(op):
+    """Compile and load the adjoint module of kernel ``op``; returns (fn, meta)."""
+    from .codegen import CudaGenerator
+    from .compiler import Compiler, Library
+    from .config import get_config
+    cfg = get_config()
+    gen = CudaGenerator(op, cfg)
+    gen.generate()  # typing, depth and struct definitions
+    ag = AdjointGenerator(gen)
+    src, sym = ag.source()
+    lib = Library(Compiler(cacheroot=cfg.cacheroot).compile(src, cfg.nvcc_flags))
+    fn = lib.entry(sym)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                   ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64), ctypes.c_void_p,
+                   ctypes.c_size_t, ctypes.c_void_p]
+    meta = {"depth": gen.depth + 1, "target": ag.slot, "nslots": len(gen.slots), "lib": lib, "T": ag.T,
+            "source": src}
+    return fn, meta
+
+
+# ------------------------------------------------------------------- autograd
+class Rollout:
+    """``steps`` forward calls of a one-sweep kernel as a differentiable map.
+
+    ``rollout = Rollout(kernel, steps, checkpoint_every=20)`` and then
+    ``u_T = rollout(u0, {"k": kappa}, (dt,))`` where ``u0`` and the coefficient
+    tensors are CUDA tensors of the grids' shape and dtype; gradients flow to
+    ``u0`` and to every coefficient tensor.  The forward pass keeps a copy of the
+    state every ``checkpoint_every`` steps; the backward pass recomputes each
+    segment from its checkpoint and runs the adjoint kernel step by step.
+    """
+
+    def __init__(self, kernel, steps: int, checkpoint_every: int = 20) -> None:
+        from .native import NativeKernel
+        if kernel.native is None:
+            kernel.native = NativeKernel(kernel)
+        self.kernel = kernel
+        self.native = kernel.native
+        self.steps = int(steps)
+        self.every = max(1, int(checkpoint_every))
+        self.fn, self.meta = build(kernel)
+        m = self.native.module
+        self.target = m.grid_args[self.meta["target"]][0]
+        self.grid_names = [n for n, _ in m.grid_args]
+        self.value_names = [n for n, _ in m.value_args]
+        self.order = m.arg_order
+        self.grids = None
+
+    def _grids(self, shape, dtype_type):
+        from .grid import Grid
+        if self.grids is None or self.grids[self.target].shape != tuple(shape):
+            self.grids = {n: Grid(tuple(shape), dtype_type) for n in self.grid_names}
+        return self.grids
+
+    def _call_args(self, grids, values):
+        out = []
+        for kind, idx in self.order:
+            out.append(grids[self.grid_names[idx]] if kind == "grid" else values[idx])
+        return out
+
+    def forward_steps(self, grids, values, count: int):
+        args = self._call_args(grids, values)
+        for _ in range(count):
+            self.kernel(*args)
+
+    def __call__(self, u0, coefs: dict, values: tuple):
+        return _RolloutFn.apply(self, tuple(values), u0, *[coefs[n] for n in self.coef_names(coefs)])
+
+    def coef_names(self, coefs: dict) -> list:
+        names = [n for n in self.grid_names if n != self.target]
+        missing = [n for n in names if n not in coefs]
+        if missing:
+            LOG.dead(f"missing coefficient tensors for {missing}")
+        return names
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class _RolloutFn:
+    """Built lazily so that importing the package does not import torch."""
+
+    _cls = None
+
+    @classmethod
+    def apply(cls, *args):
+        if cls._cls is None:
+            cls._cls = _make_function()
+        return cls._cls.apply(*args)
+
+
+def _make_function():
+    torch = _torch()
+    from . import device, runtime
+
+    class Fn(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, plan, values, u0, *coefs):
+            s = device.stream()
+            names = plan.coef_names(dict.fromkeys(plan.grid_names))
+            with torch.cuda.stream(s):
+                ftype = float
+                grids = plan._grids(u0.shape, ftype)
+                for n, t in zip(names, coefs):
+                    g = grids[n]
+                    g._extend_time(plan.meta["depth"])
+                    for lv in range(plan.meta["depth"]):
+                        g.tensor(lv).copy_(t)
+                ug = grids[plan.target]
+                ug.tensor(0).copy_(u0)
+                checkpoints = [u0.detach().clone()]
+                done = 0
+                while done < plan.steps:
+                    cnt = min(plan.every, plan.steps - done)
+                    plan.forward_steps(grids, values, cnt)
+                    done += cnt
+                    if done < plan.steps:
+                        checkpoints.append(ug.tensor(0).clone())
+                out = ug.tensor(0).clone()
+            ctx.plan, ctx.values, ctx.names = plan, values, names
+            ctx.checkpoints = checkpoints
+            ctx.save_for_backward(*coefs)
+            return out
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            plan, values, names = ctx.plan, ctx.values, ctx.names
+            coefs = ctx.saved_tensors
+            s = device.stream()
+            with torch.cuda.stream(s):
+                grids = plan._grids(grad_out.shape, float)
+                ug = grids[plan.target]
+                lam = grad_out.contiguous().clone()
+                gcoef = {n: torch.zeros_like(t) for n, t in zip(names, coefs)}
+                depth, ns = plan.meta["depth"], plan.meta["nslots"]
+                packed = plan.native.pack(list(values))
+                shape3 = (ctypes.c_int64 * 3)(*([1] * (3 - lam.dim()) + list(lam.shape)))
+                for seg in reversed(range(len(ctx.checkpoints))):
+                    start = seg * plan.every
+                    cnt = min(plan.every, plan.steps - start)
+                    states = [ctx.checkpoints[seg]]
+                    ug.tensor(0).copy_(ctx.checkpoints[seg])
+                    for _ in range(cnt - 1):
+                        plan.forward_steps(grids, values, 1)
+                        states.append(ug.tensor(0).clone())
+                    for i in reversed(range(cnt)):
+                        fields = (ctypes.c_void_p * (ns * depth))()
+                        grads = (ctypes.c_void_p * ns)()
+                        for slot, n in enumerate(plan.grid_names):
+                            if n == plan.target:
+                                for lv in range(depth):
+                                    fields[slot * depth + lv] = states[i].data_ptr()
+                            else:
+                                t = coefs[names.index(n)]
+                                for lv in range(depth):
+                                    fields[slot * depth + lv] = t.data_ptr()
+                                grads[slot] = gcoef[n].data_ptr()
+                        new = torch.empty_like(lam)
+                        rc = plan.fn(new.data_ptr(), lam.data_ptr(), fields, grads, shape3,
+                                     ctypes.byref(packed) if plan.value_names else None,
+                                     ctypes.sizeof(packed) if plan.value_names else 0, device.stream_handle())
+                        if rc != 0:
+                            LOG.dead(f"adjoint kernel failed: {runtime.last_error()}")
+                        lam = new
+            return (None, None, lam) + tuple(gcoef[n] for n in names)
+
+    return Fn
