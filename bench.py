@@ -66,6 +66,8 @@ def parse_args():
     ap.add_argument("--mixed-steps", type=int, default=500)
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--batch-steps", type=int, default=1000)
+    ap.add_argument("--adjoint-n", type=int, default=256)
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--mixed", default=None, choices=[None, "fp32", "fp16", "bf16"],
                     help="kernels mode: precision lowering of the pressure loop")
@@ -438,6 +440,86 @@ def batch_section(count: int, steps: int, seq_steps: int) -> dict:
     return out
 
 
+def adjoint_section(n: int, steps: int, every: int, torch_n: int) -> dict:
+    """3-D variable-coefficient diffusion, FP32, periodic: forward rollout and its
+    gradient w.r.t. the initial field and the diffusivity (adjoint kernels with
+    checkpoints every ``every`` steps); PyTorch autograd through the same stencil
+    on tensors at ``torch_n``^3 for comparison."""
+    import numpy as np
+    import torch
+
+    import xgrid
+    import workloads
+    from xgrid_gb300 import adjoint, device
+    from xgrid_gb300.operator import Operator
+
+    xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+               opt_level=3, overstep="wrap")
+    k = Operator(workloads.diffuse3d.func, "kernel", "diffuse3d")
+
+    def run_ours(m, nsteps):
+        u0, kap, tgt, dt = workloads.adjoint_setup(m, 2)
+        u0, kap, tgt = (torch.tensor(x, device="cuda") for x in (u0, kap, tgt))
+        ro = adjoint.Rollout(k, nsteps, every)
+        a, bb = u0.clone().requires_grad_(True), kap.clone().requires_grad_(True)
+        s = device.stream()
+        # warm-up (compile, tables)
+        ((ro(a, {"k": bb}, (dt,)) - tgt) ** 2).mean().backward()
+        a.grad = None
+        bb.grad = None
+        torch.cuda.synchronize()
+        s.synchronize()
+        t0 = time.perf_counter()
+        uT = ro(a, {"k": bb}, (dt,))
+        s.synchronize()
+        t1 = time.perf_counter()
+        loss = ((uT - tgt) ** 2).mean()
+        loss.backward()
+        torch.cuda.synchronize()
+        s.synchronize()
+        t2 = time.perf_counter()
+        return t1 - t0, t2 - t1, float(loss)
+
+    f, bwd, loss = run_ours(n, steps)
+    cells = n ** 3
+    out = {"config": f"{n}^3 FP32 periodic, {steps} steps, checkpoint every {every}, loss MSE to a random target",
+           "forward_s": f, "backward_s": bwd, "loss": loss,
+           "forward_glups": cells * steps / f / 1e9, "forward_gbs": 12.0 * cells * steps / f / 1e9,
+           "backward_glups": cells * steps / bwd / 1e9,
+           "backward_note": f"backward = {steps - (steps + every - 1) // every} recomputed forward steps + "
+                            f"{steps} adjoint steps (24 B/update)"}
+    # PyTorch autograd through the same stencil (tensors, roll), smaller grid
+    fs, bs, _ = run_ours(torch_n, steps)
+    u0, kap, tgt, dt = workloads.adjoint_setup(torch_n, 2)
+    u0, kap, tgt = (torch.tensor(x, device="cuda") for x in (u0, kap, tgt))
+
+    def tstep(u, kk):
+        acc = None
+        for d in range(3):
+            for sh in (-1, 1):
+                un, kn = torch.roll(u, -sh, d), torch.roll(kk, -sh, d)
+                term = (kk + kn) * (un - u)
+                acc = term if acc is None else acc + term
+        return u + dt * acc
+
+    def torch_run():
+        a, bb = u0.clone().requires_grad_(True), kap.clone().requires_grad_(True)
+        u = a
+        for _ in range(steps):
+            u = tstep(u, bb)
+        ((u - tgt) ** 2).mean().backward()
+
+    torch_run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    torch_run()
+    torch.cuda.synchronize()
+    tt = time.perf_counter() - t0
+    out["torch_autograd_gpu"] = {"n": torch_n, "fwd_bwd_s": tt, "ours_fwd_bwd_s": fs + bs,
+                                 "speedup": tt / (fs + bs)}
+    return out
+
+
 def algorithmic_bytes(module, group: int) -> float:
     """Bytes per cell of one launch of ``group``: distinct buffers read (not
     produced earlier in the launch) plus distinct buffers written, main sweeps
@@ -507,6 +589,8 @@ def main():
         out["mixed"] = mixed_section(args.mixed_n, args.mixed_steps)
     if rank == 0 and not args.no_batch:
         out["batched"] = batch_section(256, args.batch_steps, max(5, args.batch_steps // 50))
+    if rank == 0 and not args.no_adjoint:
+        out["adjoint"] = adjoint_section(args.adjoint_n, 200, 20, 128)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)

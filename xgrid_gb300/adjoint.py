@@ -252,13 +252,26 @@ class AdjointGenerator:
         hi = [max([0] + [o[a_] for o in allofs]) for a_ in range(3)]
         from .codegen import CELL_LOOP, TILE_PROLOGUE
 
+        from .codegen import SweepGroupEmitter
+        axis_name = SweepGroupEmitter.axis_name
+        none_mode = gen.cfg.overstep == "none"
+
         def body(fast):
             out = []
+            if not fast and not none_mode:
+                used = sorted({(ax, o) for off in allofs for ax, o in zip("zyx", off) if o})
+                ext = {"z": "p.Z", "y": "p.Y", "x": "p.X"}
+                out += [f"      const int {axis_name(ax, o)} = xg_axis(xg_overstep, {ax} + ({o}), (int){ext[ax]});"
+                        for ax, o in used]
+
             def ld(buf, off):
+                oz, oy, ox = off
                 if fast:
-                    oz, oy, ox = off
                     return f"{buf}[c + ({oz}) * sz + ({oy}) * sy + ({ox})]"
-                return f"xg_ldc({buf}, {addr(off)})"
+                if none_mode:
+                    return f"xg_ldc({buf}, {addr(off)})"
+                return (f"{buf}[(I){axis_name('z', oz)} * sz + (I){axis_name('y', oy)} * sy + "
+                        f"(I){axis_name('x', ox)}]")
             for i, off in enumerate(lam_offsets):
                 names[("lam", off)] = f"a{i}"
                 out.append(f"      const {T} a{i} = {ld('p.lam_in', off)};")
@@ -278,7 +291,7 @@ class AdjointGenerator:
                     out.append(f"      if (p.g{slot}) p.g{slot}[c] = p.g{slot}[c] + ({total});")
             return out
 
-        K = [f"template <typename I> __global__ void __launch_bounds__(256) xgk_{n}_adjoint("
+        K = [f"template <typename I> __global__ void __launch_bounds__(256, 4) xgk_{n}_adjoint("
              f"const __grid_constant__ struct xgadj_{n} p) {{"] + TILE_PROLOGUE + [
              f"  const bool fast = z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && y0 + ({lo[1]}) >= 0 && "
              f"y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;",
@@ -304,7 +317,7 @@ class AdjointGenerator:
             for lv in range(gen.depth + 1):
                 H.append(f"  p.f{slot}[{lv}] = (const {T}*)fields[{slot} * {gen.depth + 1} + {lv}];")
             H.append(f"  p.g{slot} = ({T}*)grads[{slot}];")
-        H += ["  p.tz = 1; p.ty = 8; p.tx = 32;",
+        H += ["  p.tz = 2; p.ty = 16; p.tx = 32;",
               "  p.ntz = xg_tiles_along(p.Z, p.tz); p.nty = xg_tiles_along(p.Y, p.ty); p.ntx = xg_tiles_along(p.X, p.tx);",
               "  dim3 grid, block(32, 8, 1);",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
@@ -339,7 +352,9 @@ def build(op):
     gen.generate()  # typing, depth and struct definitions
     ag = AdjointGenerator(gen)
     src, sym = ag.source()
-    lib = Library(Compiler(cacheroot=cfg.cacheroot).compile(src, cfg.nvcc_flags))
+    # the adjoint has no bit-exactness contract: let nvcc contract multiply-adds
+    flags = [f for f in cfg.nvcc_flags if f != "--fmad=false"]
+    lib = Library(Compiler(cacheroot=cfg.cacheroot).compile(src, flags))
     fn = lib.entry(sym)
     fn.restype = ctypes.c_int
     fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
