@@ -216,6 +216,18 @@ def cpu_baseline(n: int, seconds: float) -> dict:
 
 
 # ---------------------------------------------------------------- GPU side
+def replica_time(secs: float, world: int, device: str = "cuda") -> float:
+    """Slowest rank's time (replicas only: ranks run independent copies of the
+    workload and are synchronised by a barrier before and after timing)."""
+    if world <= 1:
+        return secs
+    import torch
+    t = torch.tensor([secs], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
 def gpu_bench(args, rank: int, world: int):
     import torch
 
@@ -261,11 +273,7 @@ def gpu_bench(args, rank: int, world: int):
     with ClockSampler(torch.cuda.current_device()) as clk:
         secs = timed(args.steps)
     torch.cuda.synchronize()
-    if world > 1:
-        t = torch.tensor([secs], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        secs = float(t.item())
-        torch.distributed.barrier()
+    secs = replica_time(secs, world)
     lups_rank = SWEEPS_PER_STEP * n * n * args.steps
 
     # profiled pass (eager, CUDA events around every launch)

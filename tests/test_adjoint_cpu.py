@@ -1,0 +1,45 @@
+"""Symbolic differentiation used by the adjoint generator, checked numerically
+on the CPU (no GPU): derivative expressions vs central differences."""
+import random
+
+from xgrid_gb300 import adjoint as A
+
+
+def evaluate(node, env):
+    k = node[0]
+    if k == "c":
+        return node[1]
+    if k in ("p", "l"):
+        return env[node[1]]
+    if k == "neg":
+        return -evaluate(node[1], env)
+    a, b = evaluate(node[1], env), evaluate(node[2], env)
+    return {"+": a + b, "-": a - b, "*": a * b, "/": a / b}[k]
+
+
+def test_partials_match_central_differences():
+    rng = random.Random(0)
+    L = [("l", (0, 1, (0, 0, o))) for o in (-1, 0, 1)]
+    K = [("l", (1, 0, (0, 0, o))) for o in (-1, 0, 1)]
+    dt = ("p", "dt")
+    # u' = u + dt * ((k0 + k1)(u1 - u0) + (k0 + km)(um - u0)) / (1 + k0 * k0)
+    flux = A.s_add(A.s_mul(A.s_add(K[1], K[2]), A.s_sub(L[2], L[1])),
+                   A.s_mul(A.s_add(K[1], K[0]), A.s_sub(L[0], L[1])))
+    expr = A.s_add(L[1], A.s_div(A.s_mul(dt, flux), A.s_add(("c", 1.0), A.s_mul(K[1], K[1]))))
+    env = {"dt": 0.3}
+    for n in L + K:
+        env[n[1]] = rng.uniform(0.1, 1.0)
+    for n in L + K:
+        d = A.diff(expr, n[1])
+        h = 1e-6
+        e1, e2 = dict(env), dict(env)
+        e1[n[1]] += h
+        e2[n[1]] -= h
+        fd = (evaluate(expr, e1) - evaluate(expr, e2)) / (2 * h)
+        assert abs(evaluate(d, env) - fd) < 1e-7
+
+
+def test_shift_moves_every_load():
+    node = A.s_mul(("l", (0, 1, (0, 0, 1))), ("l", (1, 0, (0, -1, 0))))
+    s = A.shift(node, (0, 0, 1))
+    assert A.loads_of(s) == [(0, 1, (0, 0, 0)), (1, 0, (0, -1, -1))]

@@ -1,0 +1,41 @@
+"""Multi-GPU mode is replicas only (the workload does not shard): ranks run
+independent replicas and the benchmark reports the slowest rank's time.  The
+rendezvous and max-reduction run here with gloo on CPU, world size 2."""
+import os
+import socket
+
+import pytest
+import torch
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    t = bench.replica_time(1.0 + rank, world, device="cpu")
+    q.put((rank, t))
+    dist.destroy_process_group()
+
+
+def test_replica_time_is_the_max_over_ranks():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(60)
+        assert p.exitcode == 0
+    res = dict(q.get(timeout=5) for _ in range(2))
+    assert res == {0: 2.0, 1: 2.0}
