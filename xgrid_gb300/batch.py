@@ -117,13 +117,20 @@ class BatchEmitter:
                  f"x1 - 1 + ({hi[2]}) < p.X;")
         for j in mains:
             K.append(f"    const bool mz{j} = p.tzero{j}[t] != 0;")
+        R = e.rows_for(mains)
         K.append("    if (fast) {")
-        K += ["  " + l for l in CELL_LOOP]
-        K += e.main_body(mains, True, "        ", mask_vars)
-        K += ["      }}", "    } else if (p.same) {"]
-        K += ["  " + l for l in CELL_LOOP]
-        K += e.main_body(mains, "edge", "        ", mask_vars)
-        K += ["      }}", "    } else {"]
+        if R:
+            K += e.rows_loop(mains[0], mask_vars[mains[0]], "      ", "fast", R)
+            K += ["    } else if (p.same) {"]
+            K += e.rows_loop(mains[0], mask_vars[mains[0]], "      ", "edge", R)
+            K += ["    } else {"]
+        else:
+            K += ["  " + l for l in CELL_LOOP]
+            K += e.main_body(mains, True, "        ", mask_vars)
+            K += ["      }}", "    } else if (p.same) {"]
+            K += ["  " + l for l in CELL_LOOP]
+            K += e.main_body(mains, "edge", "        ", mask_vars)
+            K += ["      }}", "    } else {"]
         K += ["  " + l for l in CELL_LOOP]
         K += e.main_body(mains, False, "        ", mask_vars)
         K += ["      }}", "    }", "  }", "}"]

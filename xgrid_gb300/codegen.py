@@ -983,6 +983,85 @@ class SweepGroupEmitter:
             lines.append(f"{indent}}}")
         return lines
 
+    def rows_for(self, mains: list) -> int:
+        """Rows per thread and iteration of the two-phase path (0: not used): as
+        many as the registers allow for the sweep's distinct loads."""
+        if len(mains) != 1:
+            return 0
+        s = self.g.sweeps[mains[0]]
+        if any(s.store_offset):
+            return 0
+        numeric = ("float", "double", "int8_t", "int16_t", "int32_t", "int64_t")
+        if not all(self.elem(b[0]) in numeric for b in self.buffers([s])):
+            return 0
+        nl = len(s.distinct_loads()) + (1 if s.implicit else 0)
+        return 4 if nl <= 6 else (2 if nl <= 12 else 0)
+
+    def rows_loop(self, j: int, mask_var: str, indent: str = "  ", mode: str = "fast", R: int = 4) -> list:
+        """Cell loop that walks ``R`` rows per thread and iteration in two phases:
+        every load of the rows first (predicated on the row being in the tile),
+        then the stores, so that loads of several rows are in flight together (a
+        latency-bound streaming sweep needs that to reach HBM bandwidth).
+        ``mode`` "fast": unchecked offsets (interior tiles); "edge": wrapped or
+        clamped coordinates computed per row and axis offset (edge tiles whose
+        grids share the domain's extent)."""
+        s = self.g.sweeps[j]
+        dst = self.bname((s.slot, s.level, s.write_version))
+        src = self.bname((s.slot, s.level, s.read_version_of_target))
+        none = self.gen.cfg.overstep == "none"
+        out = [f"{indent}for (int z = z0; z < z1; ++z)",
+               f"{indent}for (int yb = y0 + (int)threadIdx.y; yb < y1; yb += {R} * (int)blockDim.y)",
+               f"{indent}for (int x = x0 + (int)threadIdx.x; x < x1; x += (int)blockDim.x) {{"]
+        if mode == "edge" and not none:
+            zs = sorted({ld.offset[0] for ld in s.distinct_loads() if ld.offset[0]})
+            xs = sorted({ld.offset[2] for ld in s.distinct_loads() if ld.offset[2]})
+            out += [f"{indent}  const int {self.axis_name('z', o)} = xg_axis(xg_overstep, z + ({o}), (int)p.Z);"
+                    for o in zs]
+            out += [f"{indent}  const int {self.axis_name('x', o)} = xg_axis(xg_overstep, x + ({o}), (int)p.X);"
+                    for o in xs]
+        exprs = []
+        for r in range(R):
+            out.append(f"{indent}  const int y_{r} = yb + {r} * (int)blockDim.y;")
+            out.append(f"{indent}  const bool ok_{r} = {'true' if r == 0 else f'y_{r} < y1'};")
+            out.append(f"{indent}  const I c_{r} = (I)z * sz + (I)y_{r} * sy + (I)x;")
+            if mode == "edge" and not none:
+                ys = sorted({ld.offset[1] for ld in s.distinct_loads() if ld.offset[1]})
+                out += [f"{indent}  const int wy{r}_{'m' if o < 0 else 'p'}{abs(o)} = "
+                        f"xg_axis(xg_overstep, y_{r} + ({o}), (int)p.Y);" for o in ys]
+            names, local = {}, {}
+            for st, ld in s.loads:
+                if ld not in local:
+                    vn = f"l{len(local)}_{r}"
+                    local[ld] = vn
+                    b = self.bname((ld.slot, ld.level, ld.version))
+                    oz, oy, ox = ld.offset
+                    t = self.elem(ld.slot)
+                    if mode == "fast":
+                        off = "".join(f" + ({o}) * {m}" for o, m in ((oz, "sz"), (oy, "sy")) if o) + \
+                            (f" + ({ox})" if ox else "")
+                        ref = f"{b}[c_{r}{off}]"
+                    elif none:
+                        off = f"({oz}) * (int64_t)sz + ({oy}) * (int64_t)sy + ({ox})"
+                        ref = f"xg_ldc({b}, xg_flat((int64_t)c_{r} + {off}, (int64_t)sz * p.Z))"
+                    else:
+                        wy = f"wy{r}_{'m' if oy < 0 else 'p'}{abs(oy)}" if oy else f"y_{r}"
+                        ref = f"{b}[(I){self.axis_name('z', oz)} * sz + (I){wy} * sy + (I){self.axis_name('x', ox)}]"
+                    out.append(f"{indent}  const {t} {vn} = ok_{r} ? {ref} : ({t})0;")
+                names[id(st)] = local[ld]
+            if s.implicit:
+                t = self.elem(s.slot)
+                out.append(f"{indent}  const {t} s_{r} = ok_{r} ? {src}[c_{r}] : ({t})0;")
+            env = SweepEnv(self.gen, self.hoist_map, names, self.div_map)
+            exprs.append(self.gen.expr(s.stmt.value, env))
+        for r in range(R):
+            out.append(f"{indent}  if (ok_{r}) {{")
+            out.append(f"{indent}    if ({mask_var} || p.m{j}[c_{r}] == 0) {dst}[c_{r}] = {exprs[r]};")
+            if s.implicit:
+                out.append(f"{indent}    else {dst}[c_{r}] = s_{r};")
+            out.append(f"{indent}  }}")
+        out.append(f"{indent}}}")
+        return out
+
     def main_kernel(self, tag: str, mains: list, bnd_phases: list, final: list | None = None) -> str:
         """Tile kernel: main sweeps ``mains`` (indices into the group) then the
         boundary phases ``bnd_phases`` on the tile's own cells."""
@@ -1005,14 +1084,21 @@ class SweepGroupEmitter:
         for j in mains:
             mask_vars[j] = f"mz{j}"
             lines.append(f"  const bool mz{j} = p.tzero{j}[t] != 0;")
+        R = self.rows_for(mains)
         lines.append("  if (fast) {")
-        lines += ["  " + l for l in CELL_LOOP]
-        lines += self.main_body(mains, True, "      ", mask_vars)
-        lines.append("    }}")
+        if R:
+            lines += self.rows_loop(mains[0], mask_vars[mains[0]], "    ", "fast", R)
+        else:
+            lines += ["  " + l for l in CELL_LOOP]
+            lines += self.main_body(mains, True, "      ", mask_vars)
+            lines.append("    }}")
         lines.append("  } else if (p.same) {")
-        lines += ["  " + l for l in CELL_LOOP]
-        lines += self.main_body(mains, "edge", "      ", mask_vars)
-        lines.append("    }}")
+        if R:
+            lines += self.rows_loop(mains[0], mask_vars[mains[0]], "    ", "edge", R)
+        else:
+            lines += ["  " + l for l in CELL_LOOP]
+            lines += self.main_body(mains, "edge", "      ", mask_vars)
+            lines.append("    }}")
         lines.append("  } else {")
         lines += ["  " + l for l in CELL_LOOP]
         lines += self.main_body(mains, False, "      ", mask_vars)

@@ -268,18 +268,31 @@ class MixedLoopEmitter:
                     lo[a] = min(lo[a], ld.offset[a])
                     hi[a] = max(hi[a], ld.offset[a])
 
-        def loader(buf: str, fast: bool):
+        def loader(buf: str, fast: bool, idx: str = "c"):
             def load(st):
                 oz, oy, ox = analysis.pad3(st.space_offset)
                 if fast:
                     off = "".join(f" + ({o}) * {s}" for o, s in ((oz, "sz"), (oy, "sy")) if o) + (f" + ({ox})" if ox else "")
-                    return f"{buf}[c{off}]"
+                    return f"{buf}[{idx}{off}]"
                 return f"xg_ldc({buf}, xg_addr(xg_overstep, z, y, x, {oz}, {oy}, {ox}, p.Z, p.Y, p.X))"
             return load
 
-        def lin_code(sweep, buf, fast):
-            code = LinearEmitter(self, target, loader(buf, fast)).lin(sweep.stmt.value)
+        def lin_code(sweep, buf, fast, idx="c"):
+            code = LinearEmitter(self, target, loader(buf, fast, idx)).lin(sweep.stmt.value)
             return "0.0f" if code is None else code
+
+        R = 4
+        rows = ["    for (int z = z0; z < z1; ++z)",
+                f"    for (int yb = y0 + (int)threadIdx.y; yb < y1; yb += {R} * (int)blockDim.y)",
+                "    for (int x = x0 + (int)threadIdx.x; x < x1; x += (int)blockDim.x) {"]
+        for r in range(R):
+            rows += [f"      const int y_{r} = yb + {r} * (int)blockDim.y;",
+                     f"      const bool ok_{r} = {'true' if r == 0 else f'y_{r} < y1'};",
+                     f"      const I c_{r} = (I)z * sz + (I)y_{r} * sy + (I)x;",
+                     f"      const float v_{r} = ok_{r} ? {lin_code(main, 'din', True, f'c_{r}')} + rr[c_{r}] : 0.0f;"]
+        for r in range(R):
+            rows.append(f"      if (ok_{r}) dout[c_{r}] = v_{r};")
+        rows.append("    }")
 
         params = [f"struct xgp_{n}_{gid}_mxd {{", f"  struct xgm_{n}_{gid} k;", "  int64_t Z, Y, X;",
                   "  int32_t tz, ty, tx;", "  int64_t ntz, nty, ntx;", "  const float* din;", "  float* dout;",
@@ -298,8 +311,8 @@ class MixedLoopEmitter:
              "  float* __restrict__ dout = p.dout;",
              "  const float* __restrict__ rr = p.r;",
              "  if (fast && mz) {  // interior tile without boundary cells: one pass, r added directly"]
-        K += ["  " + l for l in loop]
-        K += [f"      dout[c] = {lin_code(main, 'din', True)} + rr[c];", "    }}", "    return;", "  }",
+        K += rows
+        K += ["    return;", "  }",
               "  if (fast) {"]
         K += ["  " + l for l in loop]
         K += [f"      dout[c] = (mz || p.m0[c] == 0) ? {lin_code(main, 'din', True)} : din[c];", "    }}",
