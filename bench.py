@@ -73,6 +73,8 @@ def parse_args():
                     help="kernels mode: precision lowering of the pressure loop")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "batch"],
                     help="kernels mode: which workload to run")
+    ap.add_argument("--temporal", default=None,
+                    help="kernels mode, batch workload: steps per launch, or depth,ty,tx (1 = none)")
     ap.add_argument("--mode", default="bench", choices=["bench", "kernels"],
                     help="kernels: only run warm-up + steps (for profiler launch lists)")
     return ap.parse_args()
@@ -87,8 +89,12 @@ def kernels_only(args) -> None:
         xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
                    opt_level=3, overstep="wrap")
         probs = workloads.batch_setup(256, seed=1)
+        temporal = None
+        if args.temporal:
+            parts = [int(x) for x in args.temporal.split(",")]
+            temporal = parts[0] if len(parts) == 1 else tuple(parts)
         for _ in range(args.warmup + 1):
-            workloads.convdiff2d.batch(probs, args.steps)
+            workloads.convdiff2d.batch(probs, args.steps, temporal=temporal)
         device.synchronize()
         print(json.dumps({"mode": "kernels", "workload": "batch", "calls": args.warmup + 1}))
         return
@@ -415,15 +421,23 @@ def batch_section(count: int, steps: int, seq_steps: int) -> dict:
     probs = workloads.batch_setup(count, seed=1)
     cells = sum(int(np.prod(p[0].shape)) for p in probs)
     s = device.stream()
-    k.batch(probs, steps)  # eager (descriptors, tables)
-    k.batch(probs, steps)  # capture
-    s.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    k.batch(probs, steps)
-    e1.record(s)
-    s.synchronize()
-    ms_b = e0.elapsed_time(e1)
+
+    def timed(temporal):
+        k.batch(probs, steps, temporal=temporal)  # eager (descriptors, tables)
+        k.batch(probs, steps, temporal=temporal)  # capture
+        s.synchronize()
+        e0.record(s)
+        k.batch(probs, steps, temporal=temporal)
+        e1.record(s)
+        s.synchronize()
+        return e0.elapsed_time(e1)
+
+    ms_1 = timed(1)
+    t0 = time.perf_counter()
+    temporal = k.native.tuned_temporal(probs)
+    tune_s = time.perf_counter() - t0
+    ms_b = timed(temporal)
     for _ in range(2):
         for args in probs:
             k(*args)
@@ -438,10 +452,15 @@ def batch_section(count: int, steps: int, seq_steps: int) -> dict:
     hbm, src = peaks()
     out = {"problems": count, "cells": cells, "steps": steps,
            "batched": {"ms": ms_b, "value": cells * steps / (ms_b * 1e-3) / 1e9, "unit": "GLUP/s",
-                       "gbs": 8.0 * cells * steps / (ms_b * 1e-3) / 1e9},
+                       "gbs": 8.0 * cells * steps / (ms_b * 1e-3) / 1e9,
+                       "temporal": {"depth": temporal[0], "tile": [temporal[1], temporal[2]],
+                                    "block": list(temporal[3]), "tuned_in_s": tune_s}},
+           "one_step_per_launch": {"ms": ms_1, "value": cells * steps / (ms_1 * 1e-3) / 1e9, "unit": "GLUP/s",
+                                   "gbs": 8.0 * cells * steps / (ms_1 * 1e-3) / 1e9},
            "per_problem_calls": {"ms": ms_s, "value": cells * steps / (ms_s * 1e-3) / 1e9, "unit": "GLUP/s",
                                  "timed_steps": seq_steps}}
     out["batched"]["hbm_frac"] = out["batched"]["gbs"] / hbm
+    out["one_step_per_launch"]["hbm_frac"] = out["one_step_per_launch"]["gbs"] / hbm
     out["speedup_vs_per_problem"] = ms_s / ms_b
     out["config"] = (f"{count} problems, extents U[64,1024] per axis (seed 1), FP32, periodic, convection-diffusion "
                      f"5-point, {steps} steps in one CUDA graph of persistent launches")

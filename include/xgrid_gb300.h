@@ -118,6 +118,9 @@ const int32_t* xg_mask_device(const xg_mask* mask);
 /* Device list of the cells (row-major linear indices, ascending) whose mask
  * equals `value` (value != 0). */
 int xg_mask_cells(xg_mask* mask, int32_t value, const int64_t** cells, int64_t* count);
+/* Number of cells whose mask is nonzero (host-side count, no device work).
+ * Runtime helper with no counterpart in the reference. */
+int xg_mask_nonzero(const xg_mask* mask, int64_t* count);
 /* Tile tables for a tiling of `tile` = {tz, ty, tx} cells (the last tile of
  * each axis absorbs the remainder):  *tile_zero[t] = 1 when every cell of tile
  * t has mask 0;  *csr_off/*csr_cells list the cells of mask `value` grouped by

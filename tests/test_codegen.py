@@ -57,8 +57,61 @@ def test_affine_degree():
 
 
 @pytest.mark.skipif(shutil.which("nvcc") is None, reason="nvcc not available")
-def test_generated_modules_compile():
+def test_generated_modules_compile(tmp_path):
     from xgrid_gb300.compiler import Compiler
     for kw in ({}, {"mixed": "fp32"}):
         m = _gen(workloads.cavity_kernel, **kw)
-        Compiler(cacheroot="/tmp/xgcg").compile(m.source, get_config().nvcc_flags)
+        Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)
+    # batched (+ temporal blocking) and adjoint modules
+    from xgrid_gb300.adjoint import AdjointGenerator
+    xgrid.init(precision="float", cacheroot="/tmp/xgcg", opt_level=3, overstep="wrap")
+    m = CudaGenerator(Operator(workloads.convdiff2d.func, "kernel", "convdiff2d"), get_config()).generate()
+    Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)
+    for fn, name in ((workloads.diffuse3d.func, "diffuse3d"), (workloads.convdiff2d.func, "convdiff2d")):
+        gen = CudaGenerator(Operator(fn, "kernel", name), get_config())
+        gen.generate()
+        src, _ = AdjointGenerator(gen).source()
+        Compiler(cacheroot=str(tmp_path)).compile(src, get_config().nvcc_flags)
+
+
+def shadowing(u: xgrid.grid[float, 2], v: xgrid.grid[float, 2], a: float, s: float, G: float, p: float,
+              h: float) -> None:
+    # argument names that the generated C also uses internally
+    u[0, 0] = a * u[0, 0] + s * u[0, 1] + G * v[-1, 0] + p * v[1, 0] + h
+    v[0, 0] = v[0, 0] + a * (u[0, -1] - v[0, 0])
+
+
+def returning(u: xgrid.grid[float, 2], ret: int, nret: int, r: float) -> int:
+    total = 0
+    i = 0
+    while i < ret:
+        i = i + 1
+        if i % 2 == 0:
+            continue
+        total = total + i
+    for j in range(0, nret):
+        u[0, 0] = u[0, 1] * r + u[0, 0]
+    return total * 3
+
+
+def test_temporal_plan_and_power_of_two_scaling():
+    m = _gen(workloads.cavity_kernel)
+    # the Jacobi sweep multiplies by dx^2, dy^2 and a coefficient: scale parameters
+    assert m.source.count("xg_make_scale(") >= 3 and "xg_mulk(" in m.source
+    xgrid.init(precision="float", cacheroot="/tmp/xgcg", opt_level=3, overstep="wrap")
+    mb = CudaGenerator(Operator(workloads.convdiff2d.func, "kernel", "convdiff2d"), get_config()).generate()
+    assert mb.batch and "xgk_convdiff2d_tb" in mb.source
+    xgrid.init(precision="float", cacheroot="/tmp/xgcg", opt_level=3, overstep="limit")
+    mn = CudaGenerator(Operator(workloads.convdiff2d.func, "kernel", "convdiff2d"), get_config()).generate()
+    assert mn.batch and "xgk_convdiff2d_tb" not in mn.source  # clamped edges do not block in time
+
+
+@pytest.mark.skipif(shutil.which("nvcc") is None, reason="nvcc not available")
+def test_argument_names_do_not_collide_with_generated_names(tmp_path):
+    from xgrid_gb300.compiler import Compiler
+    xgrid.init(precision="double", cacheroot="/tmp/xgcg", opt_level=3, overstep="wrap")
+    m = CudaGenerator(Operator(shadowing, "kernel", "shadowing"), get_config()).generate()
+    assert m.batch and "xgk_shadowing_tb" in m.source
+    Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)
+    m = CudaGenerator(Operator(returning, "kernel", "returning"), get_config()).generate()
+    Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)

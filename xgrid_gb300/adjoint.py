@@ -182,6 +182,10 @@ class AdjointGenerator:
             div = self.em.div_map.get(id(e))
             if div is not None:  # division by a launch constant: its value is the divisor's d
                 return s_div(self.to_sym(e.left), ("p", div.name + ".d"))
+            mul = self.em.mul_map.get(id(e))
+            if mul is not None:  # product with a launch constant: its value is the scale's m
+                h, other = mul
+                return s_mul(self.to_sym(other), ("p", h.name + ".m"))
             a, b = self.to_sym(e.left), self.to_sym(e.right)
             if e.operator is B.Add:
                 return s_add(a, b)
@@ -303,14 +307,17 @@ class AdjointGenerator:
         H = [f'extern "C" int xg_adjoint_{n}(void* lam_out, const void* lam_in, const void* const* fields, '
              f'void* const* grads, const int64_t* shape, const void* args, size_t nargs, void* stream) {{',
              "  cudaStream_t s = (cudaStream_t)stream;",
-             f"  struct xga_{n} a;",
-             "  memset(&a, 0, sizeof a);",
-             "  if (nargs) memcpy(&a, args, nargs < sizeof a ? nargs : sizeof a);"]
+             f"  struct xga_{n} xg_a;",
+             "  memset(&xg_a, 0, sizeof xg_a);",
+             "  if (nargs) memcpy(&xg_a, args, nargs < sizeof xg_a ? nargs : sizeof xg_a);",
+             f"  struct xgh_{n}_{self.group.index} xg_h;",
+             "  memset(&xg_h, 0, sizeof xg_h);",
+             "  {  // the kernel's arguments, by their own names, for the launch constants"]
         for an, at in value_args:
-            H.append(f"  {c_type(at)} {an} = a.{an}; (void){an};")
+            H.append(f"    {c_type(at)} {an} = xg_a.{an}; (void){an};")
         from .codegen import HostEnv
-        H += em.host_hoists(HostEnv(gen), "  ")
-        H += [f"  struct xgadj_{n} p;", "  memset(&p, 0, sizeof p);", "  p.h = h_;",
+        H += em.host_hoists(HostEnv(gen), "    ")[2:]
+        H += ["  }", f"  struct xgadj_{n} p;", "  memset(&p, 0, sizeof p);", "  p.h = xg_h;",
               "  p.Z = shape[0]; p.Y = shape[1]; p.X = shape[2];",
               f"  p.lam_in = (const {T}*)lam_in; p.lam_out = ({T}*)lam_out;"]
         for slot in slots_used:

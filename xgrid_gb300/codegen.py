@@ -199,6 +199,10 @@ class CudaGenerator:
         div = getattr(env, "div_map", {}).get(id(e))
         if div is not None:
             return f"xg_divk((double)({self.expr(e.left, env)}), p.h.{div.name})"
+        mul = getattr(env, "mul_map", {}).get(id(e))
+        if mul is not None:
+            h, other = mul
+            return f"xg_mulk((double)({self.expr(other, env)}), p.h.{h.name})"
         if isinstance(e, ir.Constant):
             return literal(e.value)
         if isinstance(e, ir.Identifier):
@@ -597,18 +601,21 @@ class CudaGenerator:
         return out
 
     def host_entry(self, name, entry, value_args, rtype, d, lines) -> list[str]:
-        out = [f'extern "C" int {entry}(xg_grid* G, int ngrids, const void* args, size_t nargs, void* ret, '
-               f'size_t nret, void* stream) {{',
-               "  cudaStream_t s = (cudaStream_t)stream;",
-               f"  if (ngrids != {len(self.slots)}) XG_FAIL(\"{name}: expected {len(self.slots)} grids, got %d\", ngrids);",
-               f"  struct xga_{name} a;",
-               f"  if (nargs != {'sizeof(a)' if value_args else '0'}) XG_FAIL(\"{name}: argument block has %zu bytes, "
-               f"expected %zu\", nargs, (size_t){'sizeof(a)' if value_args else '0'});",
-               "  memset(&a, 0, sizeof a);",
-               "  if (nargs) memcpy(&a, args, nargs);",
-               "  (void)ret; (void)nret; (void)s;"]
+        # generated names in the entry's scope start with xg_ (reserved), so kernel
+        # arguments and locals keep their own names, as inline C expects
+        out = [f'extern "C" int {entry}(xg_grid* xg_G, int xg_ngrids, const void* xg_args, size_t xg_nargs, '
+               f'void* xg_ret, size_t xg_nret, void* xg_stream) {{',
+               "  cudaStream_t xg_s = (cudaStream_t)xg_stream;",
+               f"  if (xg_ngrids != {len(self.slots)}) XG_FAIL(\"{name}: expected {len(self.slots)} grids, got %d\", "
+               f"xg_ngrids);",
+               f"  struct xga_{name} xg_a;",
+               f"  if (xg_nargs != {'sizeof(xg_a)' if value_args else '0'}) XG_FAIL(\"{name}: argument block has %zu "
+               f"bytes, expected %zu\", xg_nargs, (size_t){'sizeof(xg_a)' if value_args else '0'});",
+               "  memset(&xg_a, 0, sizeof xg_a);",
+               "  if (xg_nargs) memcpy(&xg_a, xg_args, xg_nargs);",
+               "  (void)xg_ret; (void)xg_nret; (void)xg_s;"]
         for an, at in value_args:
-            out.append(f"  {c_type(at)} {an} = a.{an};")
+            out.append(f"  {c_type(at)} {an} = xg_a.{an};")
         for vn, var in d.scope.items():
             if vn not in d.signature.argnames_map:
                 out.append(f"  {self.use_type(var.type)} {vn};")
@@ -636,14 +643,14 @@ class HostEnv:
         slot = gen.slots[e.variable.name]
         if e.info == "dimension":
             return str(e.variable.type.dimension)
-        return f"((int32_t)G[{slot}].shape[{gen.expr(e.dimension, self)}])"
+        return f"((int32_t)xg_G[{slot}].shape[{gen.expr(e.dimension, self)}])"
 
     def ret(self, gen, s: ir.Return, indent: str) -> list[str]:
         if s.value is None:
             return [f"{indent}return 0;"]
         t = c_type(s.value.type)
-        return [f"{indent}{{ {t} r_ = {gen.expr(s.value, self)};",
-                f"{indent}  if (ret && nret == sizeof r_) memcpy(ret, &r_, sizeof r_);",
+        return [f"{indent}{{ {t} xg_r = {gen.expr(s.value, self)};",
+                f"{indent}  if (xg_ret && xg_nret == sizeof xg_r) memcpy(xg_ret, &xg_r, sizeof xg_r);",
                 f"{indent}  return 0; }}"]
 
 
@@ -676,6 +683,7 @@ class Hoisted:
     ctype: str
     expr: ir.Expression
     divisor: bool = False  # an xg_divisor built from ``expr`` on the host
+    scale: bool = False    # an xg_scale (multiplier) built from ``expr`` on the host
 
 
 class SweepEnv:
@@ -684,11 +692,13 @@ class SweepEnv:
 
     device = True
 
-    def __init__(self, gen, hoisted: dict, loadnames: dict, div_map: dict | None = None) -> None:
+    def __init__(self, gen, hoisted: dict, loadnames: dict, div_map: dict | None = None,
+                 mul_map: dict | None = None) -> None:
         self.gen = gen
         self.hoisted = hoisted
         self.loadnames = loadnames
         self.div_map = div_map or {}
+        self.mul_map = mul_map or {}
 
     def substitute(self, e):
         h = self.hoisted.get(id(e))
@@ -721,15 +731,17 @@ class SweepGroupEmitter:
         self.hoisted: list[Hoisted] = []
         self.hoist_map: dict = {}
         self.div_map: dict = {}
+        self.mul_map: dict = {}
         self.by_text: dict = {}  # (kind, host C text) -> Hoisted: equal subtrees share one parameter
 
-    def _param(self, e: ir.Expression, divisor: bool) -> "Hoisted":
+    def _param(self, e: ir.Expression, divisor: bool, scale: bool = False) -> "Hoisted":
         text = self.gen.expr(e, HostEnv(self.gen))
-        key = ("k" if divisor else "v", text)
+        key = ("k" if divisor else ("s" if scale else "v"), text)
         h = self.by_text.get(key)
         if h is None:
             name = f"{key[0]}{len(self.hoisted)}"
-            h = Hoisted(name, "xg_divisor" if divisor else self.gen.ctype(e), e, divisor)
+            ctype = "xg_divisor" if divisor else ("xg_scale" if scale else self.gen.ctype(e))
+            h = Hoisted(name, ctype, e, divisor, scale)
             self.hoisted.append(h)
             self.by_text[key] = h
         return h
@@ -751,6 +763,13 @@ class SweepGroupEmitter:
                 # x / d with d fixed for the launch: precomputed reciprocal pair on the host
                 self.div_map[id(e)] = self._param(e.right, True)
                 self.hoist(e.left, conditional)
+                return
+            if (e.operator is ir.BinaryOperator.Mul and self.gen.cfg.divisor and self.gen.ctype(e) == "double"
+                    and has_stencil(e.left) != has_stencil(e.right)):
+                # x * m with m fixed for the launch: exponent arithmetic when m is +-2^s
+                inv, other = (e.right, e.left) if has_stencil(e.left) else (e.left, e.right)
+                self.mul_map[id(e)] = (self._param(inv, False, True), other)
+                self.hoist(other, conditional)
                 return
             cond = conditional or e.operator.is_logic()
             self.hoist(e.left, conditional)
@@ -774,7 +793,7 @@ class SweepGroupEmitter:
         self.prepare()
         out.append(f"{indent}{{")
         out.extend(self.host_hoists(env, indent + "  "))
-        out.append(f"{indent}  XG_TRY(xgl_{self.name}_{self.gid}(G, &h_, s));")
+        out.append(f"{indent}  XG_TRY(xgl_{self.name}_{self.gid}(xg_G, &xg_h, xg_s));")
         out.append(f"{indent}}}")
         self.emit_kernels()
 
@@ -783,14 +802,16 @@ class SweepGroupEmitter:
             self.hoist(s.stmt.value)
 
     def host_hoists(self, env, indent: str) -> list:
-        """Host lines declaring ``h_`` and evaluating every hoisted subtree."""
+        """Host lines declaring ``xg_h`` and evaluating every hoisted subtree."""
         gen, n, gid = self.gen, self.name, self.gid
-        out = [f"{indent}struct xgh_{n}_{gid} h_;", f"{indent}memset(&h_, 0, sizeof h_);"]
+        out = [f"{indent}struct xgh_{n}_{gid} xg_h;", f"{indent}memset(&xg_h, 0, sizeof xg_h);"]
         for h in self.hoisted:
             if h.divisor:
-                out.append(f"{indent}h_.{h.name} = xg_make_divisor((double)({gen.expr(h.expr, env)}));")
+                out.append(f"{indent}xg_h.{h.name} = xg_make_divisor((double)({gen.expr(h.expr, env)}));")
+            elif h.scale:
+                out.append(f"{indent}xg_h.{h.name} = xg_make_scale((double)({gen.expr(h.expr, env)}));")
             else:
-                out.append(f"{indent}h_.{h.name} = {gen.expr(h.expr, env)};")
+                out.append(f"{indent}xg_h.{h.name} = {gen.expr(h.expr, env)};")
         return out
 
     def emit_kernels(self) -> None:
@@ -955,7 +976,7 @@ class SweepGroupEmitter:
                 local[ld] = vn
                 lines.append(f"{indent}const {self.elem(ld.slot)} {vn} = {self.load_code(sweep, ld, fast)};")
             names[id(st)] = local[ld]
-        env = SweepEnv(self.gen, self.hoist_map, names, self.div_map)
+        env = SweepEnv(self.gen, self.hoist_map, names, self.div_map, self.mul_map)
         return lines, self.gen.expr(sweep.stmt.value, env)
 
     def main_body(self, sweeps_idx: list, fast, indent: str, mask_vars: dict) -> list:
@@ -1051,7 +1072,7 @@ class SweepGroupEmitter:
             if s.implicit:
                 t = self.elem(s.slot)
                 out.append(f"{indent}  const {t} s_{r} = ok_{r} ? {src}[c_{r}] : ({t})0;")
-            env = SweepEnv(self.gen, self.hoist_map, names, self.div_map)
+            env = SweepEnv(self.gen, self.hoist_map, names, self.div_map, self.mul_map)
             exprs.append(self.gen.expr(s.stmt.value, env))
         for r in range(R):
             out.append(f"{indent}  if (ok_{r}) {{")

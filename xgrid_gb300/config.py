@@ -25,6 +25,9 @@ Backend options (new keywords, all optional):
 * ``fuse``: fuse consecutive sweeps into one launch where the masks allow it.
 * ``divisor``: precompute loop-invariant divisors on the host and divide with a
   correctly rounded multiply/FMA sequence (checked per divisor).
+* ``autotune``: pick the batched path's temporal-block depth and tile shape by
+  timing candidates on the first call for a set of problem shapes (cached on disk
+  in ``cacheroot``; see ``xgrid_gb300.autotune``).
 """
 from __future__ import annotations
 
@@ -56,6 +59,7 @@ class Configuration:
     fuse: bool = True
     divisor: bool = True
     mixed_every: int = 0
+    autotune: bool = True
 
     def __repr__(self) -> str:
         return repr(dataclasses.asdict(self))
@@ -85,7 +89,7 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
          comment: bool = False, overstep: Literal["none", "limit", "wrap"] = "none",
          opt_level: Literal[0, 1, 2, 3] = 2, precision: Literal["float", "double"] = "float",
          exact: bool = True, mixed: Optional[str] = None, graph: bool = True,
-         fuse: bool = True, divisor: bool = True, mixed_every: int = 0) -> None:
+         fuse: bool = True, divisor: bool = True, mixed_every: int = 0, autotune: bool = True) -> None:
     """Set the global configuration (same keywords as the reference plus GPU options)."""
     global _config
     if sys.version_info < (3, 10):
@@ -99,5 +103,5 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
     if opt_level not in (0, 1, 2, 3):
         logger.dead(f"Invalid opt_level '{opt_level}'")
     _config = Configuration(parallel, list(cc), cacheroot, comment, overstep, opt_level,
-                            precision, exact, mixed, graph, fuse, divisor, int(mixed_every))
+                            precision, exact, mixed, graph, fuse, divisor, int(mixed_every), bool(autotune))
     logger.info(f"initialized with configuration: {_config}")

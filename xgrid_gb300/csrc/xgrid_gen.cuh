@@ -60,10 +60,51 @@ XG_HD float xg_sq_f(float a) { return a * a; }
 // window of x exponents where that holds; outside it (and for d not normal,
 // x = 0, inf, NaN, tiny or huge) the IEEE division runs instead, so the result
 // is RN(x/d) for every x.
+// Multiplication by a launch-invariant factor m.  When m = +-2^s the product is
+// exact unless it leaves the normal range, so for a normal x with a normal
+// result it is x with s added to its exponent (and the sign flipped for m < 0):
+// integer instructions only, which matters where the FP64 pipe bounds a sweep.
+// Zeros keep their magnitude; subnormal or out-of-range products, inf and NaN
+// take the FP64 multiply.  Either way the result is RN(x*m).
+struct xg_scale {
+  double m;
+  int s;             // exponent of |m| when p2
+  unsigned hs;       // s << 20: added to the high word of x
+  unsigned sg;       // sign bit of m, in the high word
+  int p2;            // |m| is a power of two
+};
+
+static inline xg_scale xg_make_scale(double m) {
+  xg_scale k;
+  memset(&k, 0, sizeof k);
+  k.m = m;
+  if (!isfinite(m) || m == 0.0 || fpclassify(m) != FP_NORMAL) return k;
+  int ex = 0;
+  const double fr = frexp(m, &ex);  // |fr| in [0.5, 1)
+  if (fabs(fr) != 0.5) return k;
+  k.s = ex - 1;
+  k.hs = (unsigned)k.s << 20;
+  k.sg = m < 0 ? 0x80000000u : 0u;
+  k.p2 = 1;
+  return k;
+}
+
+__device__ __forceinline__ double xg_mulk(double x, const xg_scale& k) {
+  if (k.p2) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    if (e - 1u <= 2045u && (unsigned)((int)e + k.s - 1) <= 2045u)
+      return __hiloint2double((int)((hi + k.hs) ^ k.sg), (int)lo);
+    if (((hi << 1) | lo) == 0u) return __hiloint2double((int)(hi ^ k.sg), (int)lo);
+  }
+  return __dmul_rn(x, k.m);
+}
+
 struct xg_divisor {
   double d, zh, zl;
   unsigned lo, span;  // fast path when (biased exponent of x) - lo <= span (unsigned)
   int ok;
+  xg_scale rz;        // d = +-2^s: x/d = x * 2^-s exactly (rz.p2 set)
 };
 
 static inline xg_divisor xg_make_divisor(double d) {
@@ -73,6 +114,7 @@ static inline xg_divisor xg_make_divisor(double d) {
   if (!isfinite(d) || d == 0.0 || fpclassify(d) != FP_NORMAL) return k;
   const double zh = 1.0 / d;
   if (!isfinite(zh) || fpclassify(zh) != FP_NORMAL) return k;
+  if (fma(-zh, d, 1.0) == 0.0) k.rz = xg_make_scale(zh);  // 1/d exact: a power of two
   const double e = fma(-zh, d, 1.0);  // 1 - zh*d, exact for zh = RN(1/d)
   k.zh = zh;
   k.zl = e / d;
@@ -90,6 +132,7 @@ static inline xg_divisor xg_make_divisor(double d) {
 }
 
 __device__ __forceinline__ double xg_divk(double x, const xg_divisor& k) {
+  if (k.rz.p2) return xg_mulk(x, k.rz);  // x/d and x*(1/d) are the same real number
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
   if (k.ok && e - k.lo <= k.span) {

@@ -262,6 +262,14 @@ int xg_mask_cells(xg_mask* m, int32_t value, const int64_t** cells, int64_t* cou
   return 0;
 }
 
+int xg_mask_nonzero(const xg_mask* m, int64_t* count) {
+  if (!m || !count) return fail("xg_mask_nonzero: null argument");
+  int64_t n = 0;
+  for (const auto& kv : m->cells) n += static_cast<int64_t>(kv.second.size());
+  *count = n;
+  return 0;
+}
+
 int xg_mask_tiles(xg_mask* m, const int32_t* tile, int32_t value, const uint8_t** tile_zero,
                   const int32_t** csr_off, const int64_t** csr_cells, int64_t* ntiles) {
   if (!m || !tile) return fail("xg_mask_tiles: null argument");

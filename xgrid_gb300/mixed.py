@@ -236,22 +236,22 @@ class MixedLoopEmitter:
         v = plan.loop.variable.name
         out.append(f"{indent}{{")
         out.extend(b.host_hoists(env, indent + "  "))
-        out.append(f"{indent}  struct xgm_{n}_{gid} hm_;")
-        out.append(f"{indent}  memset(&hm_, 0, sizeof hm_);")
+        out.append(f"{indent}  struct xgm_{n}_{gid} xg_hm;")
+        out.append(f"{indent}  memset(&xg_hm, 0, sizeof xg_hm);")
         for name, text, kind in self.coefs:
             if kind == "mul":
-                out.append(f"{indent}  hm_.{name} = (float)({text});")
+                out.append(f"{indent}  xg_hm.{name} = (float)({text});")
             else:
-                out.append(f"{indent}  hm_.{name} = (float)(1.0 / (double)({text}));")
+                out.append(f"{indent}  xg_hm.{name} = (float)(1.0 / (double)({text}));")
         lp = plan.loop
         out.append(f"{indent}  int64_t xg_K = 0;")
         out.append(f"{indent}  for ({v} = {gen.expr(lp.start, env)}; {v} < {gen.expr(lp.end, env)}; "
                    f"{v} += {gen.expr(lp.step, env)}) ++xg_K;")
         out.append(f"{indent}  if (xg_K > 0) {{")
-        out.append(f"{indent}    int xg_mx = xgm_{n}_{gid}_ready(G);")
+        out.append(f"{indent}    int xg_mx = xgm_{n}_{gid}_ready(xg_G);")
         out.append(f"{indent}    if (xg_mx < 0) return xg_mx;")
-        out.append(f"{indent}    if (xg_mx) XG_TRY(xgm_{n}_{gid}_run(G, &h_, &hm_, xg_K, s));")
-        out.append(f"{indent}    else for (int64_t xg_i = 0; xg_i < xg_K; ++xg_i) XG_TRY(xgl_{n}_{gid}(G, &h_, s));")
+        out.append(f"{indent}    if (xg_mx) XG_TRY(xgm_{n}_{gid}_run(xg_G, &xg_h, &xg_hm, xg_K, xg_s));")
+        out.append(f"{indent}    else for (int64_t xg_i = 0; xg_i < xg_K; ++xg_i) XG_TRY(xgl_{n}_{gid}(xg_G, &xg_h, xg_s));")
         out.append(f"{indent}  }}")
         out.append(f"{indent}}}")
 

@@ -124,8 +124,20 @@ class NativeKernel:
         return packed
 
     # --------------------------------------------------------------- batched
-    def batch(self, problems, steps: int = 1) -> None:
-        """Batched execution (see ``xgrid_gb300.batch``)."""
+    def set_temporal(self, depth: int, ty: int = 32, tx: int = 64, block: tuple = (32, 8, 1)) -> None:
+        """Temporal blocking of the batched path: ``depth`` steps per launch (1 turns
+        it off) on tiles of ``ty`` x ``tx`` cells, CTAs of ``block`` threads."""
+        if depth < 1 or ty < 1 or tx < 1:
+            self.logger.dead("temporal blocking: depth, ty and tx must be positive")
+        self._temporal = (int(depth), int(ty), int(tx), tuple(int(b) for b in block))
+
+    def temporal_supported(self) -> bool:
+        return self.module.batch and hasattr(self.lib.dylib, f"xg_batch_tb_{self.module.name}")
+
+    def batch(self, problems, steps: int = 1, temporal=None) -> None:
+        """Batched execution (see ``xgrid_gb300.batch``).  ``temporal`` overrides
+        the kernel's temporal-blocking setting for this call: a ``(depth, ty, tx)``
+        tuple, or 1 to run one step per launch."""
         if not self.module.batch:
             self.logger.dead(f"kernel '{self.module.name}' cannot run batched: its body must be one run of "
                              f"explicit mask-0 grid assignments")
@@ -147,6 +159,10 @@ class NativeKernel:
                            "blocks": blocks_fn, "fn": ctypes.cast(fn, ctypes.c_void_p).value, "desc": {},
                            "counters": None, "nblocks": {}}
         B = self._batch
+        if (temporal is None and getattr(self, "_temporal", None) is None and self.config.autotune
+                and steps >= 2 and self.temporal_supported()):
+            temporal = self.tuned_temporal(problems)
+        tb = self._temporal_for(temporal, steps)
         all_grids, all_values = [], []
         for args in problems:
             grids, values = self.split(tuple(args))
@@ -157,7 +173,7 @@ class NativeKernel:
         uploaded = False
         for g in all_grids:
             g._extend_time(B["depth"])
-            uploaded |= g._sync_device(False)
+            uploaded |= g._sync_device(tb is not None)
         if uploaded:
             device.stream().synchronize()
         nprob = len(problems)
@@ -167,25 +183,34 @@ class NativeKernel:
         stride = ctypes.sizeof(self.args_type) if self.module.value_args else 0
         tiling = self._tiling_key(B["group"])
         key = (tuple((st.level[k] or 0) for st in arr for k in range(B["depth"])),
+               tuple((st.scratch or 0) if tb else 0 for st in arr),
                tuple(st.mask or 0 for st in arr), tuple(runtime.load().xg_mask_version(st.mask) for st in arr),
-               packed, tiling)
+               packed, tiling, tb[:3] if tb else None)
         entry = B["desc"].get(key)
         if entry is None:
-            host = ctypes.create_string_buffer(nprob * (B["dsize"] + 8))
-            total, maxc = ctypes.c_int64(), ctypes.c_int64()
+            host = ctypes.create_string_buffer(nprob * (B["dsize"] + 16))
+            total, maxc, total_tb = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(-1)
             args_buf = ctypes.create_string_buffer(packed, max(len(packed), 1))
+            tbcfg = (ctypes.c_int32 * 3)(*tb[:3]) if tb else None
             rc = B["prep"](arr, ctypes.c_int(nprob), args_buf, ctypes.c_size_t(stride), host,
-                           ctypes.c_size_t(len(host)), ctypes.byref(total), ctypes.byref(maxc))
+                           ctypes.c_size_t(len(host)), ctypes.byref(total), ctypes.byref(maxc), tbcfg,
+                           ctypes.byref(total_tb))
             if rc != 0:
                 self.logger.dead(f"batch preparation failed: {runtime.last_error()}")
+            if tb and total_tb.value < 0:
+                self.logger.info(f"temporal blocking not used: {runtime.last_error()}")
             t = device.torch()
             dev = device.alloc_bytes(len(host))
             with t.cuda.stream(device.stream()):
                 dev[: len(host)].copy_(t.frombuffer(bytearray(host.raw), dtype=t.uint8), non_blocking=False)
             if len(B["desc"]) > 16:
                 B["desc"].clear()
-            entry = B["desc"][key] = (dev, total.value, maxc.value)
-        dev, total, maxc = entry
+            entry = B["desc"][key] = (dev, total.value, maxc.value, total_tb.value)
+        dev, total, maxc, total_tb = entry
+        if tb and total_tb >= 0:
+            self._batch_temporal(B, tb, dev, total_tb, steps, nprob, maxc)
+            self._after_batch(all_grids, steps, B["depth"])
+            return
         if B["counters"] is None or B["counters"].numel() < steps * 8:
             B["counters"] = device.alloc_bytes(steps * 8)
         block = tiling[3:6]
@@ -201,18 +226,82 @@ class NativeKernel:
                                     ctypes.sizeof(ba), None, 0, device.stream_handle(), 1 if self.use_graph else 0)
         if rc != 0:
             self.logger.dead(f"batched kernel '{self.module.name}' failed: {runtime.last_error()}")
-        for g in all_grids:
+        self._after_batch(all_grids, steps, B["depth"])
+
+    def tuned_temporal(self, problems) -> tuple:
+        """The autotuner's (depth, ty, tx, block) for these problems' shapes."""
+        shapes = tuple(tuple(a.shape for a in args if isinstance(a, Grid)) for args in problems)
+        memo = self.__dict__.setdefault("_tuned", {})
+        if shapes not in memo:
+            from . import autotune
+            memo[shapes] = autotune.tune_batch(self, problems)
+        return memo[shapes]
+
+    def _after_batch(self, grids, steps: int, depth: int) -> None:
+        for g in grids:
             if self.op.tick:
-                for _ in range(steps % B["depth"]):
+                for _ in range(steps % depth):
                     g._levels.insert(0, g._levels.pop())
             for lv in g._levels:
                 lv.auth = "dev"
+
+    def _temporal_for(self, temporal, steps: int):
+        """(depth, ty, tx, block) of this call's temporal blocking, or None."""
+        if steps < 2 or not self.temporal_supported():
+            return None
+        if temporal is None:
+            cfg = getattr(self, "_temporal", None)
+            if cfg is None:
+                cfg = DEFAULT_TEMPORAL
+        elif isinstance(temporal, int):
+            cfg = (temporal, 32, 64, (32, 8, 1))
+        else:
+            t = tuple(temporal)
+            cfg = t + ((32, 8, 1),) if len(t) == 3 else t
+        if cfg[0] <= 1:
+            return None
+        return (int(cfg[0]), int(cfg[1]), int(cfg[2]), tuple(int(b) for b in cfg[3]))
+
+    def _batch_temporal(self, B, tb, dev, total_tb: int, steps: int, nprob: int, maxc: int) -> None:
+        depth, ty, tx, block = tb
+        threads = block[0] * block[1] * block[2]
+        ck = (threads,) + tb[:3]
+        if ck not in B["nblocks"]:
+            fn = getattr(self.lib.dylib, f"xg_batch_tb_blocks_{self.module.name}")
+            fn.restype = ctypes.c_int
+            smem, nb = ctypes.c_int(), ctypes.c_int()
+            if fn(ctypes.c_int(threads), ctypes.c_int(depth), ctypes.c_int(ty), ctypes.c_int(tx),
+                  ctypes.byref(smem), ctypes.byref(nb)) != 0:
+                self.logger.dead(runtime.last_error())
+            B["nblocks"][ck] = (smem.value, nb.value)
+        smem, nb = B["nblocks"][ck]
+        if B["counters"] is None or B["counters"].numel() < steps * 8:
+            B["counters"] = device.alloc_bytes(steps * 8)
+        fn = ctypes.cast(getattr(self.lib.dylib, f"xg_batch_tb_{self.module.name}"), ctypes.c_void_p).value
+        ba = BatchTemporalArgs(dev.data_ptr(), total_tb, steps, B["counters"].data_ptr(), nprob,
+                               1 if maxc < (1 << 31) - 1 else 0, nb, depth, ty, tx, smem,
+                               (ctypes.c_int32 * 3)(*block))
+        rc = runtime.load().xg_call(fn, None, 0, ctypes.cast(ctypes.byref(ba), ctypes.c_void_p),
+                                    ctypes.sizeof(ba), None, 0, device.stream_handle(), 1 if self.use_graph else 0)
+        if rc != 0:
+            self.logger.dead(f"batched kernel '{self.module.name}' failed: {runtime.last_error()}")
 
     def _tiling_key(self, group: int) -> tuple:
         arr = (ctypes.c_int32 * 6)()
         getter = getattr(self.lib.dylib, f"xg_get_tiling_{self.module.name}")
         getter(ctypes.c_int(group), arr)
         return tuple(arr)
+
+
+# steps per launch, tile rows, tile columns, CTA shape of the temporally blocked batched path
+DEFAULT_TEMPORAL = (4, 32, 56, (32, 8, 1))
+
+
+class BatchTemporalArgs(ctypes.Structure):
+    _fields_ = [("desc", ctypes.c_void_p), ("total", ctypes.c_int64), ("steps", ctypes.c_int64),
+                ("counters", ctypes.c_void_p), ("nprob", ctypes.c_int32), ("small", ctypes.c_int32),
+                ("blocks", ctypes.c_int32), ("T", ctypes.c_int32), ("ty", ctypes.c_int32), ("tx", ctypes.c_int32),
+                ("smem", ctypes.c_int32), ("block", ctypes.c_int32 * 3)]
 
 
 class BatchArgs(ctypes.Structure):

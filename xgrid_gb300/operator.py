@@ -44,15 +44,18 @@ class Operator:
             return self.func(*args)
         self.logger.dead(f"Invalid call to non-kernel or non-function ({self.mode}) operator '{self.name}'")
 
-    def batch(self, problems, steps: int = 1) -> None:
+    def batch(self, problems, steps: int = 1, temporal=None) -> None:
         """Run ``steps`` calls of this kernel on each of ``problems`` (argument
-        tuples of independent problems) with one persistent launch per step."""
+        tuples of independent problems) with one persistent launch per step, or
+        per ``depth`` steps when the kernel can be temporally blocked
+        (``temporal``: ``(depth, ty, tx)``, 1 for none; default: the kernel's
+        setting, else the tuned or built-in one)."""
         if self.mode != "kernel":
             self.logger.dead(f"Only kernels can be batched, '{self.name}' is a {self.mode}")
         if self.native is None:
             from .native import NativeKernel
             self.native = NativeKernel(self)
-        return self.native.batch(problems, steps)
+        return self.native.batch(problems, steps, temporal)
 
     @property
     def ir(self) -> ir.Definition:
