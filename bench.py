@@ -65,6 +65,8 @@ def parse_args():
     ap.add_argument("--mixed-n", type=int, default=4097)
     ap.add_argument("--mixed-steps", type=int, default=500)
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mixed-temporal", type=int, default=4,
+                    help="defect iterations per launch of the mixed-precision loop (0: one per launch)")
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--adjoint-n", type=int, default=256)
     ap.add_argument("--no-adjoint", action="store_true")
@@ -99,7 +101,7 @@ def kernels_only(args) -> None:
         print(json.dumps({"mode": "kernels", "workload": "batch", "calls": args.warmup + 1}))
         return
     xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
-               opt_level=3, mixed=args.mixed)
+               opt_level=3, mixed=args.mixed, mixed_temporal=args.mixed_temporal)
     grids, cfg = workloads.cavity_setup(args.n, stable_dt(args.n))
     for _ in range(args.warmup + args.steps):
         workloads.cavity_kernel(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
@@ -355,11 +357,13 @@ def gpu_bench(args, rank: int, world: int):
     return result
 
 
-def mixed_section(n: int, steps: int) -> dict:
-    """Cavity at n^2 for ``steps`` steps: plain FP64 vs FP32 defect iterations with
-    FP64 residual/correction (``mixed="fp32"``), same initial state; steps/s of
-    each (CUDA events over the second half of the run; fields exceed L2) and the
-    error of p, u, v against the FP64 run."""
+def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
+    """Cavity at n^2 for ``steps`` steps: plain FP64 vs defect iterations with
+    FP64 residual/correction (``mixed`` = "fp32", "fp16", "bf16": storage of the
+    defect between launches, FP32 arithmetic, ``temporal`` iterations per
+    launch), same initial state; steps/s of each (CUDA events over the second
+    half of the run; fields exceed L2) and the error of p, u, v against the FP64
+    run."""
     import numpy as np
     import torch
 
@@ -370,9 +374,9 @@ def mixed_section(n: int, steps: int) -> dict:
 
     dt = stable_dt(n)
     out, fields = {}, {}
-    for mode in (None, "fp32"):
+    for mode in (None, "fp32", "fp16", "bf16"):
         xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
-                   opt_level=3, mixed=mode)
+                   opt_level=3, mixed=mode, mixed_temporal=temporal)
         k = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
         grids, cfg = workloads.cavity_setup(n, dt)
         args = (grids["b"], grids["p"], grids["u"], grids["v"], cfg)
@@ -391,15 +395,18 @@ def mixed_section(n: int, steps: int) -> dict:
         out["fp64" if mode is None else mode] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms,
                                                  "value": SWEEPS_PER_STEP * n * n / (ms * 1e-3) / 1e9,
                                                  "unit": "GLUP/s"}
-    err = {}
-    for g in "puv":
-        a, ref = fields["fp32"][g], fields[None][g]
-        err[g] = {"max_rel": float(np.abs(a - ref).max() / np.abs(ref).max()),
-                  "l2_rel": float(np.linalg.norm(a - ref) / np.linalg.norm(ref))}
-    out["fp32"]["error_vs_fp64"] = err
-    out["fp32"]["speedup_vs_fp64"] = out["fp64"]["ms_per_step"] / out["fp32"]["ms_per_step"]
-    out["config"] = f"cavity {n}x{n}, dt={dt:g}, {steps} steps from zero fields; FP32 defect sweeps, " \
-                    f"FP64 source, residual, correction and projection; one correction per 50-iteration loop"
+    for mode in ("fp32", "fp16", "bf16"):
+        err = {}
+        for g in "puv":
+            a, ref = fields[mode][g], fields[None][g]
+            err[g] = {"max_rel": float(np.abs(a - ref).max() / np.abs(ref).max()),
+                      "l2_rel": float(np.linalg.norm(a - ref) / np.linalg.norm(ref))}
+        out[mode]["error_vs_fp64"] = err
+        out[mode]["speedup_vs_fp64"] = out["fp64"]["ms_per_step"] / out[mode]["ms_per_step"]
+    out["config"] = (f"cavity {n}x{n}, dt={dt:g}, {steps} steps from zero fields; defect iterations in FP32 "
+                     f"arithmetic ({temporal} per launch, TMA-staged tiles; fp16/bf16: 16-bit storage with a "
+                     f"power-of-two scale per field), FP64 source, residual, correction and projection; one "
+                     f"correction per 50-iteration loop")
     return out
 
 
@@ -613,7 +620,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     out = gpu_bench(args, rank, world)
     if rank == 0 and not args.no_mixed:
-        out["mixed"] = mixed_section(args.mixed_n, args.mixed_steps)
+        out["mixed"] = mixed_section(args.mixed_n, args.mixed_steps, args.mixed_temporal)
     if rank == 0 and not args.no_batch:
         out["batched"] = batch_section(256, args.batch_steps, max(5, args.batch_steps // 50))
     if rank == 0 and not args.no_adjoint:

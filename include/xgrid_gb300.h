@@ -133,6 +133,26 @@ int xg_mask_tiles(xg_mask* mask, const int32_t* tile, int32_t value,
  * lies in the same tile as c (reads outside the grid count as local). */
 int xg_mask_tile_local(xg_mask* mask, const int32_t* tile, int32_t value, int noff,
                        const int32_t* offsets, int overstep, int* ok);
+/* Box tables of temporally blocked launches (runtime helpers with no
+ * counterpart in the reference, which sweeps once per statement).  Tiles have
+ * exactly core = {tz, ty, tx} cells (the last tile of an axis may reach past
+ * the grid) and are read with halo = {hz, hy, hx} cells per side (the "box").
+ * *box_zero[t] = 1 when every grid cell in tile t's box has mask 0; for
+ * value != 0, *off (ntiles+1 entries) and *local list per tile the cells of
+ * mask `value` inside its box as box-local indices ((z*BY + y)*BX + x). */
+int xg_mask_boxes(xg_mask* mask, const int32_t* core, const int32_t* halo, int32_t value,
+                  const uint8_t** box_zero, const int32_t** off, const int32_t** local,
+                  int64_t* ntiles);
+/* 1 in *ok when `depth` iterations of an in-place sweep group can run inside
+ * each box without reading stale cells: every mask-0 cell's `nmain` offsets
+ * (nmain x 3, z,y,x) stay in the grid; and for each of the `nphase` boundary
+ * phases (mask values[p], noffs[p] offsets, consecutive in `offsets`), every
+ * read of a cell of that value stays in the grid, reads no cell of the same
+ * value, and lies no closer to an inner box edge than the cell itself (up to
+ * depth * shrink[a] along axis a, shrink being the main sweep's reach). */
+int xg_mask_box_check(xg_mask* mask, const int32_t* core, const int32_t* halo, const int32_t* shrink,
+                      int32_t depth, int nmain, const int32_t* main_offsets, int nphase,
+                      const int32_t* values, const int32_t* noffs, const int32_t* offsets, int* ok);
 
 /* ---- graph-cached calls -------------------------------------------------- */
 /* Call `fn` and cache the launches it makes as a CUDA graph keyed by the

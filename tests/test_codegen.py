@@ -43,8 +43,21 @@ def test_divisors_are_precomputed_and_deduplicated():
 
 def test_mixed_matches_cavity_pressure_loop():
     m = _gen(workloads.cavity_kernel, mixed="fp32")
-    assert m.aux_per_cell == {1: 12}
+    assert m.aux_per_cell == {1: 14}
     assert "_mxd(" in m.source and "_mxc(" in m.source
+
+
+def test_mixed_loop_has_temporal_tma_kernel():
+    """2-D loops get the temporally blocked defect kernel: TMA box loads on an
+    mbarrier, storage type per mode, the tile's boundary phases from box lists."""
+    for mode, dt in (("fp32", "float"), ("fp16", "__half"), ("bf16", "__nv_bfloat16")):
+        m = _gen(workloads.cavity_kernel, mixed=mode)
+        assert "xgk_cavity_kernel_1_mxt" in m.source
+        assert "xg_tma_load_2d(" in m.source and "xg_mbar_wait(" in m.source
+        assert f"xgk_cavity_kernel_1_mxt<{dt}, RS>" in m.source
+        assert m.source.count("xg_mask_boxes(") == 5  # box-zero flags + four boundary phases
+    hdr = open(__import__("xgrid_gb300").build.CSRC + "/xgrid_gen.cuh").read()
+    assert "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes" in hdr
 
 
 def test_affine_degree():
@@ -59,7 +72,7 @@ def test_affine_degree():
 @pytest.mark.skipif(shutil.which("nvcc") is None, reason="nvcc not available")
 def test_generated_modules_compile(tmp_path):
     from xgrid_gb300.compiler import Compiler
-    for kw in ({}, {"mixed": "fp32"}):
+    for kw in ({}, {"mixed": "fp32"}, {"mixed": "bf16"}, {"mixed": "fp16"}):
         m = _gen(workloads.cavity_kernel, **kw)
         Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)
     # batched (+ temporal blocking) and adjoint modules

@@ -172,3 +172,22 @@ def test_temporal_blocking_falls_back_for_masks_and_small_extents(cacheroot):
     kb.batch(a, 9, temporal=(8, 8, 8))   # halo 8 > extents of 5..7
     _sequential(ks, b, 9)
     _same_levels(a, b)
+
+
+def test_temporal_configurations_in_any_order(cacheroot):
+    """Configurations of different shared-memory sizes, one after the other and
+    each replayed from its CUDA graph: a larger tile after a smaller one (same
+    depth and tile, other CTA shape) still launches and gives the same bits."""
+    xgrid.init(precision="float", cacheroot=cacheroot, opt_level=3, overstep="wrap")
+    kb = Operator(workloads.convdiff2d.func, "kernel", "convdiff2d")
+    ks = Operator(workloads.convdiff2d.func, "kernel", "convdiff2d")
+    a = _problems(15, 8, 70, 200)
+    b = _problems(15, 8, 70, 200)
+    total = 0
+    for cfg in ((2, 32, 124, (32, 8, 1)), (2, 64, 60, (32, 8, 1)), (2, 32, 124, (64, 4, 1)),
+                (2, 32, 124, (32, 8, 1))):
+        for _ in range(3):  # eager, capture, replay
+            kb.batch(a, 4, temporal=cfg)
+            total += 4
+    _sequential(ks, b, total)
+    _same_levels(a, b)

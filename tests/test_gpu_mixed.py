@@ -28,7 +28,7 @@ def _rel(a, b):
 def test_mixed_cavity_within_1e8_of_fp64(cacheroot, every):
     ref, _ = _cavity(cacheroot, 257, 60, 1e-5, None)
     out, k = _cavity(cacheroot, 257, 60, 1e-5, "fp32", every)
-    assert k.native.module.aux_per_cell == {1: 12}
+    assert k.native.module.aux_per_cell == {1: 14}
     for g in "puv":
         assert np.isfinite(out[g]).all()
         assert _rel(out[g], ref[g]) < 1e-8, g
@@ -77,7 +77,7 @@ def test_mixed_falls_back_when_boundary_reads_cross_tiles(cacheroot):
     # mask-1 cells in column 31 read column 32, which belongs to the next 32-wide tile
     ref, _ = _relax_run(cacheroot, None, 31)
     out, k = _relax_run(cacheroot, "fp32", 31)
-    assert k.native.module.aux_per_cell == {0: 12}
+    assert k.native.module.aux_per_cell == {0: 14}
     assert out.tobytes() == ref.tobytes()
 
 

@@ -1,0 +1,96 @@
+"""Temporally blocked defect iterations of the mixed-precision pressure loop
+(TMA-staged boxes, several iterations per launch).  With FP32 storage the
+result has the same bits as one iteration per launch, for every depth and
+strip height, on square and non-square grids with odd extents; with 16-bit
+storage (FP16 / BF16 and a power-of-two scale per field) the pressure stays
+within the storage format's tolerance of the FP64 path.  The staging copies
+never time out (error word of the work area stays 0)."""
+import numpy as np
+import pytest
+
+import xgrid
+import workloads
+from xgrid_gb300 import device, mixed, runtime
+from xgrid_gb300.operator import Operator
+
+pytestmark = pytest.mark.gpu
+
+
+def cavity_grids(ny, nx, dt):
+    """Lid-driven cavity on ny x nx points (masks as in the cavity example)."""
+    grids = {k: xgrid.Grid((ny, nx), float) for k in "bpuv"}
+    m = {k: np.zeros((ny, nx), np.int32) for k in "bpuv"}
+    m["u"][0, :] = 1
+    m["u"][:, 0] = 1
+    m["u"][:, -1] = 1
+    m["u"][-1, :] = 2
+    m["v"].fill(1)
+    m["v"][1:-1, 1:-1] = 0
+    m["p"][:, -1] = 1
+    m["p"][0, :] = 2
+    m["p"][:, 0] = 3
+    m["p"][-1, :] = 4
+    m["b"].fill(1)
+    m["b"][1:-1, 1:-1] = 0
+    for k in "bpuv":
+        grids[k].boundary[...] = m[k]
+    return grids, workloads.Config(1.0, 0.1, dt, 2.0 / (nx - 1), 2.0 / (ny - 1))
+
+
+def kernel(cacheroot, mode):
+    xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3, mixed=mode)
+    return Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
+
+
+def run(k, shape, steps, temporal, rows=16, dt=1e-5):
+    if k.native is None:
+        from xgrid_gb300.native import NativeKernel
+        k.native = NativeKernel(k)
+    k.native.set_mixed_temporal(temporal, rows)
+    grids, cfg = cavity_grids(*shape, dt)
+    lib = runtime.load()
+    lib.xg_prof_reset()
+    for _ in range(steps):
+        k(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+    launches = lib.xg_prof_launches()
+    out = {g: grids[g].read(0) for g in "puv"}
+    device.stream().synchronize()
+    word = int(grids["p"]._aux[mixed.aux_error_offset(grids["p"].shape):][:4].cpu().numpy().view(np.int32)[0])
+    return out, launches, word
+
+
+@pytest.mark.parametrize("shape", [(257, 257), (203, 333)])
+@pytest.mark.parametrize("temporal,rows", [(4, 16), (3, 8), (1, 16), (6, 16), (8, 24)])
+def test_fp32_temporal_equals_one_iteration_per_launch(cacheroot, shape, temporal, rows):
+    k = kernel(cacheroot, "fp32")
+    ref, n_ref, _ = run(k, shape, 6, 0)
+    out, n_tb, word = run(k, shape, 6, temporal, rows)
+    for g in "puv":
+        assert out[g].tobytes() == ref[g].tobytes(), g
+    assert word == 0
+    # 49 defect launches per step become ceil(49 / temporal)
+    assert n_tb < n_ref or temporal == 1
+
+
+@pytest.mark.parametrize("mode,tol", [("fp16", 2e-3), ("bf16", 1e-2)])
+def test_16bit_storage_within_tolerance_of_fp64(cacheroot, mode, tol):
+    xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3)
+    k64 = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
+    grids, cfg = cavity_grids(257, 257, 1e-5)
+    for _ in range(30):
+        k64(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+    ref = {g: grids[g].read(0) for g in "puv"}
+    k = kernel(cacheroot, mode)
+    out, _, word = run(k, (257, 257), 30, 4)
+    assert word == 0
+    errs = {}
+    for g in "puv":
+        assert np.isfinite(out[g]).all(), g
+        errs[g] = float(np.abs(out[g] - ref[g]).max() / np.abs(ref[g]).max())
+    assert errs["p"] < tol, errs
+    assert errs["u"] < tol and errs["v"] < tol, errs
+    assert out["p"].tobytes() != ref["p"].tobytes()
+    # boundary cells keep their FP64 rule exactly: copies of their neighbours, zero on the bottom row
+    p = out["p"]
+    assert (p[-1, :] == 0.0).all()
+    assert (p[1:-1, -1] == p[1:-1, -2]).all() and (p[1:-1, 0] == p[1:-1, 1]).all()

@@ -204,16 +204,14 @@ class BatchEmitter:
              f'int* blocks) {{',
              "  if (T < 1 || ty < 1 || tx < 1) XG_FAIL(\"temporal blocking: T, ty and tx must be positive\");",
              f"  const size_t bytes = xg_tb_smem_{n}(T, ty, tx);",
-             "  int dev = 0, sms = 0, per = 0, cap = 0;",
+             "  int dev = 0, sms = 0, per = 0, cap = 0, cap64 = 0;",
              "  XG_CUDA(cudaGetDevice(&dev));",
              "  XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));",
-             "  XG_CUDA(cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));",
+             f"  XG_TRY(xg_smem_optin(xgk_{n}_tb<int>, &cap));",
+             f"  XG_TRY(xg_smem_optin(xgk_{n}_tb<int64_t>, &cap64));",
+             "  if (cap64 < cap) cap = cap64;",
              "  if (bytes > (size_t)cap) XG_FAIL(\"temporal blocking: %zu bytes of shared memory per CTA exceed "
              "the %d available\", bytes, cap);",
-             f"  XG_CUDA(cudaFuncSetAttribute(xgk_{n}_tb<int>, cudaFuncAttributeMaxDynamicSharedMemorySize, "
-             "(int)bytes));",
-             f"  XG_CUDA(cudaFuncSetAttribute(xgk_{n}_tb<int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, "
-             "(int)bytes));",
              f"  XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, xgk_{n}_tb<int>, block_threads, bytes));",
              "  if (per < 1) XG_FAIL(\"temporal blocking: no CTA of %d threads and %zu bytes fits an SM\", "
              "block_threads, bytes);",

@@ -324,6 +324,7 @@ class CudaGenerator:
                 self.block(s.body, env, indent + "  ", out, ret_mode)
                 out.append(f"{indent}}}")
             elif isinstance(s, ir.For) and self.mixed_plan(s) is not None:
+                from . import mixed
                 from .mixed import MixedLoopEmitter
                 plan = self.mixed_plan(s)
                 for sw in plan.group.sweeps:
@@ -331,7 +332,7 @@ class CudaGenerator:
                         self.depth = max(self.depth, abs(st.time_offset))
                     self.depth = max(self.depth, sw.level)
                 self.sweeps.extend(plan.group.sweeps)
-                self.mixed_slots[plan.slot] = 12
+                self.mixed_slots[plan.slot] = mixed.AUX_BYTES_PER_CELL
                 MixedLoopEmitter(self, plan).emit(env, indent, out)
             elif isinstance(s, ir.For):
                 v = s.variable.name
@@ -1083,7 +1084,7 @@ class SweepGroupEmitter:
         out.append(f"{indent}}}")
         return out
 
-    def main_kernel(self, tag: str, mains: list, bnd_phases: list, final: list | None = None) -> str:
+    def main_kernel(self, tag: str, mains: list, bnd_phases: list, final=None) -> str:
         """Tile kernel: main sweeps ``mains`` (indices into the group) then the
         boundary phases ``bnd_phases`` on the tile's own cells."""
         n, gid = self.name, self.gid
@@ -1142,9 +1143,12 @@ class SweepGroupEmitter:
             lines.append(f"    {dst}[c] = {val};")
             lines += ["    }", "  }"]
         if final:
-            lines += ["  __syncthreads();"] + CELL_LOOP
-            lines += ["    " + l for l in final]
+            # a list of per-cell lines, or (lines before the cell loop, per-cell lines, lines after it)
+            pre, body, post = final if isinstance(final, tuple) else ([], final, [])
+            lines += ["  __syncthreads();"] + ["  " + l for l in pre] + CELL_LOOP
+            lines += ["    " + l for l in body]
             lines.append("  }}")
+            lines += ["  " + l for l in post]
         lines.append("}")
         return "\n".join(lines)
 
@@ -1252,7 +1256,7 @@ class SweepGroupEmitter:
         self.gen.host_chunks.append("\n".join(L))
 
     def emit_fused(self, tag: str = "fused", extra_params: list | None = None, extra_args: str = "",
-                   extra_fill: list | None = None, final: list | None = None, swap: bool = True) -> None:
+                   extra_fill: list | None = None, final=None, swap: bool = True) -> None:
         """Fused launch of the whole group.  The variant hooks (extra parameters,
         a final per-cell phase, no level exchange) serve the mixed-precision
         residual launch."""

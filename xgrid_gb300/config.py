@@ -19,8 +19,15 @@ Backend options (new keywords, all optional):
   backend; ``False`` lets the compilers contract multiply-adds (results within
   1e-12 relative of the exact path).
 * ``mixed``: ``None`` (plain), ``"fp32"``, ``"fp16"`` or ``"bf16"``: run the
-  iterations of affine in-place (Jacobi) loops on an FP32/FP16/BF16 defect with
-  FP64 residual and correction passes (see ``xgrid_gb300.mixed``).
+  iterations of affine in-place (Jacobi) loops on a defect field with FP32
+  arithmetic and FP64 residual and correction passes (see ``xgrid_gb300.mixed``).
+  ``"fp16"`` and ``"bf16"`` store the defect and the residual between launches
+  in 16 bits with a power-of-two scale per field.
+* ``mixed_temporal``: defect iterations per launch of the temporally blocked
+  defect kernel (TMA-staged tile + halo in shared memory); 0 runs one iteration
+  per launch without shared-memory staging (FP32 storage).
+* ``mixed_rows``: rows per thread of that kernel (8, 16 or 24; the tile is
+  128 columns by twice this many rows, halo included).
 * ``graph``: capture each distinct kernel call into a CUDA graph and replay it.
 * ``fuse``: fuse consecutive sweeps into one launch where the masks allow it.
 * ``divisor``: precompute loop-invariant divisors on the host and divide with a
@@ -42,6 +49,7 @@ logger = Logger("xgrid")
 _OVERSTEP = ("none", "limit", "wrap")
 _PRECISION = ("float", "double")
 _MIXED = (None, "fp32", "fp16", "bf16")
+MIXED_ROWS = (8, 16, 24)
 
 
 @dataclasses.dataclass
@@ -60,6 +68,8 @@ class Configuration:
     divisor: bool = True
     mixed_every: int = 0
     autotune: bool = True
+    mixed_temporal: int = 4
+    mixed_rows: int = 16
 
     def __repr__(self) -> str:
         return repr(dataclasses.asdict(self))
@@ -89,7 +99,8 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
          comment: bool = False, overstep: Literal["none", "limit", "wrap"] = "none",
          opt_level: Literal[0, 1, 2, 3] = 2, precision: Literal["float", "double"] = "float",
          exact: bool = True, mixed: Optional[str] = None, graph: bool = True,
-         fuse: bool = True, divisor: bool = True, mixed_every: int = 0, autotune: bool = True) -> None:
+         fuse: bool = True, divisor: bool = True, mixed_every: int = 0, autotune: bool = True,
+         mixed_temporal: int = 4, mixed_rows: int = 16) -> None:
     """Set the global configuration (same keywords as the reference plus GPU options)."""
     global _config
     if sys.version_info < (3, 10):
@@ -102,6 +113,11 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
         logger.dead(f"Invalid mixed precision '{mixed}', expected one of {_MIXED}")
     if opt_level not in (0, 1, 2, 3):
         logger.dead(f"Invalid opt_level '{opt_level}'")
+    if not 0 <= int(mixed_temporal) <= 16:
+        logger.dead(f"Invalid mixed_temporal {mixed_temporal}: 0 (off) to 16 iterations per launch")
+    if int(mixed_rows) not in MIXED_ROWS:
+        logger.dead(f"Invalid mixed_rows {mixed_rows}, expected one of {MIXED_ROWS}")
     _config = Configuration(parallel, list(cc), cacheroot, comment, overstep, opt_level,
-                            precision, exact, mixed, graph, fuse, divisor, int(mixed_every), bool(autotune))
+                            precision, exact, mixed, graph, fuse, divisor, int(mixed_every), bool(autotune),
+                            int(mixed_temporal), int(mixed_rows))
     logger.info(f"initialized with configuration: {_config}")

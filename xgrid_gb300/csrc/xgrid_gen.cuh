@@ -2,6 +2,9 @@
 // xgrid_gb300.codegen writes into the cache root).  Device code here is the
 // addressing of the stencil templates; host code is the launch plumbing.
 #pragma once
+#include <cuda.h>  // CUtensorMap and its enums only; the encoder is reached through the runtime
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdbool.h>
@@ -280,5 +283,180 @@ static inline int xg_tile_grid(int64_t ntx, int64_t nty, int64_t ntz, dim3* grid
     return -1;
   }
   *grid = dim3((unsigned)ntx, (unsigned)nty, (unsigned)ntz);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-memory-accelerator (TMA) staging of 2-D boxes into shared memory.
+//
+// A box of bx x by elements at (x, y) of a row-pitched 2-D array lands in
+// shared memory as by rows of bx elements; elements outside the array read as
+// zero.  Rules the callers keep: the array base is 16-byte aligned, the pitch
+// and bx * element size are multiples of 16 bytes, and every x coordinate times
+// the element size is a multiple of 16 bytes (negative x included).
+typedef CUresult (*xg_tmap_encode_fn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                      const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                      CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static inline int xg_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType type, int elem, int64_t X,
+                             int64_t Y, int64_t pitch_bytes, int bx, int by) {
+  static xg_tmap_encode_fn enc = NULL;
+  if (!enc) {
+    void* fn = NULL;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    XG_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !fn) XG_FAIL("cuTensorMapEncodeTiled is not available from the driver");
+    enc = (xg_tmap_encode_fn)fn;
+  }
+  if (((uintptr_t)base & 15) || (pitch_bytes & 15) || ((bx * elem) & 15) || bx > 256 || by > 256 || X < 1 || Y < 1)
+    XG_FAIL("TMA box: base %p, pitch %lld B, box %d x %d of %d-byte elements breaks the alignment rules", base,
+            (long long)pitch_bytes, bx, by, elem);
+  const cuuint64_t dims[2] = {(cuuint64_t)X, (cuuint64_t)Y};
+  const cuuint64_t strides[1] = {(cuuint64_t)pitch_bytes};
+  const cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
+  const cuuint32_t step[2] = {1, 1};
+  const CUresult r = enc(map, type, 2, (void*)base, dims, strides, box, step, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) XG_FAIL("cuTensorMapEncodeTiled failed with status %d", (int)r);
+  return 0;
+}
+
+__device__ __forceinline__ unsigned xg_smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void xg_mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(xg_smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void xg_mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(xg_smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void xg_tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          xg_smem_addr(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(xg_smem_addr(bar))
+      : "memory");
+}
+
+// Poll phase `parity` of an mbarrier at most `limit` times; false when it did not complete.
+#define XG_WAIT_LIMIT (1u << 22)
+__device__ __forceinline__ bool xg_mbar_wait(uint64_t* bar, unsigned parity, unsigned limit) {
+  for (unsigned i = 0; i < limit; ++i) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(xg_smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// Power-of-two storage scales of 16-bit fields.  For a field whose largest
+// magnitude is m, xg_scale_exp(m, A) = A - floor(log2 m) (clamped to the normal
+// exponent range), so m * 2^s lies in [2^A, 2^(A+1)); multiplying by 2^s and by
+// 2^-s is exact in FP32.  Zero, inf and NaN give s = 0.
+__device__ __forceinline__ int xg_scale_exp(float m, int A) {
+  const int b = __float_as_int(m);
+  if (!(m > 0.f) || b >= 0x7f800000) return 0;
+  const int s = A - (((b >> 23) & 0xff) - 127);
+  return s < -126 ? -126 : (s > 126 ? 126 : s);
+}
+
+__device__ __forceinline__ float xg_pow2f(int s) { return __int_as_float((s + 127) << 23); }
+
+template <typename T>
+__device__ __forceinline__ T xg_to_store(float v);
+template <>
+__device__ __forceinline__ float xg_to_store<float>(float v) {
+  return v;
+}
+template <>
+__device__ __forceinline__ __half xg_to_store<__half>(float v) {
+  return __float2half_rn(v);
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 xg_to_store<__nv_bfloat16>(float v) {
+  return __float2bfloat16_rn(v);
+}
+__device__ __forceinline__ float xg_from_store(float v) { return v; }
+__device__ __forceinline__ float xg_from_store(__half v) { return __half2float(v); }
+__device__ __forceinline__ float xg_from_store(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// Largest value over the block (every thread calls it; v >= 0 or NaN) folded
+// into *dst with an integer atomicMax (non-negative floats order like their bits).
+__device__ __forceinline__ void xg_block_max_atomic(float v, float* dst) {
+  __shared__ float red[32];
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nthr = blockDim.x * blockDim.y * blockDim.z;
+  for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  if (tid == 0) {
+    float m = 0.f;
+    for (int w = 0; w < (nthr + 31) / 32; ++w) m = fmaxf(m, red[w]);
+    atomicMax((int*)dst, __float_as_int(m));
+  }
+}
+
+// Work area of a mixed-precision loop in xg_grid.aux: the FP32 residual, two
+// defect buffers of FP32 size, a 16-bit copy of the residual, then a block of
+// per-launch maxima with an error word at its end.  Rows are padded to a
+// multiple of 32 elements so that TMA boxes can address them.
+#define XG_MX_PITCH 32
+#define XG_MX_SLOT_BYTES 65536
+struct xg_mx_aux {
+  float* r32;
+  void* dA;
+  void* dB;
+  void* r16;
+  float* slots;
+  int* err;
+  int64_t XP, nslots;
+};
+
+static inline size_t xg_align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static inline int xg_mx_layout(const xg_grid* g, xg_mx_aux* a) {
+  const xg_ext e = xg_extent(g);
+  a->XP = (e.x + XG_MX_PITCH - 1) / XG_MX_PITCH * XG_MX_PITCH;
+  const size_t np = (size_t)(e.z * e.y) * (size_t)a->XP;
+  const size_t o_dA = xg_align256(np * 4), o_dB = o_dA + xg_align256(np * 4), o_r16 = o_dB + xg_align256(np * 4);
+  const size_t o_sl = o_r16 + xg_align256(np * 2), total = o_sl + XG_MX_SLOT_BYTES;
+  if (!g->aux || (size_t)g->aux_bytes < total)
+    XG_FAIL("mixed-precision work area has %lld bytes, %zu needed", (long long)g->aux_bytes, total);
+  unsigned char* b = (unsigned char*)g->aux;
+  a->r32 = (float*)b;
+  a->dA = b + o_dA;
+  a->dB = b + o_dB;
+  a->r16 = b + o_r16;
+  a->slots = (float*)(b + o_sl);
+  a->nslots = XG_MX_SLOT_BYTES / 4 - 1;
+  a->err = (int*)(b + o_sl + XG_MX_SLOT_BYTES - 4);
+  return 0;
+}
+
+__device__ __forceinline__ int xg_clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Raise a kernel's dynamic shared-memory limit to the most the device allows
+// next to the kernel's static shared memory; *avail receives that limit.  The
+// limit is a property of the function, shared by every later launch and graph
+// replay, so it is set to the maximum once rather than to one launch's size.
+template <typename K>
+static inline int xg_smem_optin(K* kernel, int* avail) {
+  int dev = 0, cap = 0;
+  XG_CUDA(cudaGetDevice(&dev));
+  XG_CUDA(cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  XG_CUDA(cudaFuncGetAttributes(&fa, kernel));
+  const int dyn = cap - (int)fa.sharedSizeBytes;
+  XG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  if (avail) *avail = dyn;
   return 0;
 }

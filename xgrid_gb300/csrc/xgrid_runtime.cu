@@ -81,6 +81,28 @@ struct Tiles {
   std::map<int32_t, Csr> csr;
 };
 
+// Tiling of exactly `core` cells per tile (ceil division: the last tile of an
+// axis may reach past the grid), each tile read with `halo` extra cells per side.
+struct BoxKey {
+  int32_t core[3], halo[3];
+  bool operator<(const BoxKey& o) const {
+    return std::lexicographical_compare(core, core + 3, o.core, o.core + 3) ||
+           (std::equal(core, core + 3, o.core) && std::lexicographical_compare(halo, halo + 3, o.halo, o.halo + 3));
+  }
+};
+
+struct BoxCsr {
+  int32_t* off = nullptr;
+  int32_t* local = nullptr;
+};
+
+struct Boxes {
+  int64_t ntiles = 0;
+  int64_t nt[3] = {1, 1, 1};
+  uint8_t* zero = nullptr;
+  std::map<int32_t, BoxCsr> csr;
+};
+
 }  // namespace
 
 struct xg_mask {
@@ -93,6 +115,7 @@ struct xg_mask {
   std::map<int32_t, std::vector<int64_t>> cells;      // nonzero value -> sorted cells
   std::map<int32_t, int64_t*> cells_dev;
   std::map<TileKey, Tiles> tiles;
+  std::map<BoxKey, Boxes> boxes;
   std::map<std::string, int> local_cache;
 
   void release_tables() {
@@ -106,6 +129,14 @@ struct xg_mask {
       }
     }
     tiles.clear();
+    for (auto& kv : boxes) {
+      cudaFree(kv.second.zero);
+      for (auto& c : kv.second.csr) {
+        cudaFree(c.second.off);
+        cudaFree(c.second.local);
+      }
+    }
+    boxes.clear();
     local_cache.clear();
   }
 };
@@ -141,6 +172,26 @@ int64_t address(const xg_mask* m, int64_t lin, const int32_t* o, int overstep) {
     }
   }
   return (c[0] * Y + c[1]) * X + c[2];
+}
+
+// Range of tile indices along one axis whose box [i*c - h, i*c + c + h) holds coordinate x.
+inline void box_range(int64_t x, int32_t c, int32_t h, int64_t nt, int64_t* lo, int64_t* hi) {
+  // i*c - h <= x          ->  i <= floor((x + h) / c)
+  // x < i*c + c + h       ->  i*c > x - c - h  ->  i >= floor((x - c - h) / c) + 1
+  const int64_t a = x - c - h;
+  const int64_t fl = a >= 0 ? a / c : -((-a + c - 1) / c);
+  *lo = std::max<int64_t>(fl + 1, 0);
+  *hi = std::min<int64_t>((x + h) / c, nt - 1);
+}
+
+// Distance of coordinate x to the nearest box edge that lies inside the grid
+// (cells beyond it are not in the box but exist in the grid), or a large value.
+inline int64_t inner_distance(int64_t x, int64_t i, int32_t c, int32_t h, int64_t n) {
+  const int64_t lo = i * c - h, hi = i * c + c + h;
+  int64_t d = INT64_MAX / 4;
+  if (lo > 0) d = std::min<int64_t>(d, x - lo);
+  if (hi < n) d = std::min<int64_t>(d, hi - 1 - x);
+  return d;
 }
 
 // ---------------------------------------------------------------- graph cache
@@ -342,6 +393,163 @@ int xg_mask_tile_local(xg_mask* m, const int32_t* tile, int32_t value, int noff,
       for (int k = 0; k < noff && result; ++k) {
         int64_t t = address(m, c, offsets + 3 * k, overstep);
         if (t >= 0 && tile_id(m, T, key, t) != own) result = 0;
+      }
+      if (!result) break;
+    }
+  }
+  m->local_cache.emplace(ck, result);
+  *ok = result;
+  return 0;
+}
+
+int xg_mask_boxes(xg_mask* m, const int32_t* core, const int32_t* halo, int32_t value, const uint8_t** box_zero,
+                  const int32_t** off, const int32_t** local, int64_t* ntiles) {
+  if (!m || !core || !halo) return fail("xg_mask_boxes: null argument");
+  for (int a = 0; a < 3; ++a)
+    if (core[a] < 1 || halo[a] < 0) return fail("xg_mask_boxes: core extents must be positive, halos non-negative");
+  const int64_t box[3] = {core[0] + 2LL * halo[0], core[1] + 2LL * halo[1], core[2] + 2LL * halo[2]};
+  if (box[0] * box[1] * box[2] > INT32_MAX) return fail("xg_mask_boxes: box too large");
+  BoxKey key;
+  std::copy(core, core + 3, key.core);
+  std::copy(halo, halo + 3, key.halo);
+  auto it = m->boxes.find(key);
+  if (it == m->boxes.end()) {
+    Boxes B;
+    for (int a = 0; a < 3; ++a) B.nt[a] = (m->ext[a] + core[a] - 1) / core[a];
+    B.ntiles = B.nt[0] * B.nt[1] * B.nt[2];
+    if (B.ntiles > INT32_MAX) return fail("xg_mask_boxes: too many tiles");
+    std::vector<uint8_t> zero(B.ntiles, 1);
+    for (auto& kv : m->cells)
+      for (int64_t c : kv.second) {
+        const int64_t co[3] = {c / (m->ext[1] * m->ext[2]), (c / m->ext[2]) % m->ext[1], c % m->ext[2]};
+        int64_t lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) box_range(co[a], core[a], halo[a], B.nt[a], &lo[a], &hi[a]);
+        for (int64_t iz = lo[0]; iz <= hi[0]; ++iz)
+          for (int64_t iy = lo[1]; iy <= hi[1]; ++iy)
+            for (int64_t ix = lo[2]; ix <= hi[2]; ++ix) zero[(iz * B.nt[1] + iy) * B.nt[2] + ix] = 0;
+      }
+    if (upload(zero, &B.zero)) return -1;
+    it = m->boxes.emplace(key, B).first;
+  }
+  Boxes& B = it->second;
+  if (box_zero) *box_zero = B.zero;
+  if (ntiles) *ntiles = B.ntiles;
+  if (value != 0 && (off || local)) {
+    auto c = B.csr.find(value);
+    if (c == B.csr.end()) {
+      std::vector<std::pair<int64_t, int32_t>> tagged;
+      auto cv = m->cells.find(value);
+      if (cv != m->cells.end())
+        for (int64_t cell : cv->second) {
+          const int64_t co[3] = {cell / (m->ext[1] * m->ext[2]), (cell / m->ext[2]) % m->ext[1], cell % m->ext[2]};
+          int64_t lo[3], hi[3];
+          for (int a = 0; a < 3; ++a) box_range(co[a], core[a], halo[a], B.nt[a], &lo[a], &hi[a]);
+          for (int64_t iz = lo[0]; iz <= hi[0]; ++iz)
+            for (int64_t iy = lo[1]; iy <= hi[1]; ++iy)
+              for (int64_t ix = lo[2]; ix <= hi[2]; ++ix) {
+                const int64_t lz = co[0] - (iz * core[0] - halo[0]), ly = co[1] - (iy * core[1] - halo[1]),
+                              lx = co[2] - (ix * core[2] - halo[2]);
+                tagged.emplace_back((iz * B.nt[1] + iy) * B.nt[2] + ix, (int32_t)((lz * box[1] + ly) * box[2] + lx));
+              }
+        }
+      std::sort(tagged.begin(), tagged.end());
+      std::vector<int32_t> offs(B.ntiles + 1, 0), locs;
+      locs.reserve(tagged.size());
+      for (auto& p : tagged) {
+        offs[p.first + 1] += 1;
+        locs.push_back(p.second);
+      }
+      for (int64_t t = 0; t < B.ntiles; ++t) offs[t + 1] += offs[t];
+      if (offs[B.ntiles] < 0 || tagged.size() > (size_t)INT32_MAX) return fail("xg_mask_boxes: too many cells");
+      BoxCsr csr;
+      if (upload(offs, &csr.off) || upload(locs, &csr.local)) return -1;
+      c = B.csr.emplace(value, csr).first;
+    }
+    if (off) *off = c->second.off;
+    if (local) *local = c->second.local;
+  }
+  return 0;
+}
+
+int xg_mask_box_check(xg_mask* m, const int32_t* core, const int32_t* halo, const int32_t* shrink, int32_t depth,
+                      int nmain, const int32_t* main_offsets, int nphase, const int32_t* values, const int32_t* noffs,
+                      const int32_t* offsets, int* ok) {
+  if (!m || !core || !halo || !shrink || !ok || (nmain > 0 && !main_offsets) ||
+      (nphase > 0 && (!values || !noffs)))
+    return fail("xg_mask_box_check: null argument");
+  std::string ck("box");
+  auto put = [&ck](const void* p, size_t b) { ck.append(static_cast<const char*>(p), b); };
+  put(core, 12);
+  put(halo, 12);
+  put(shrink, 12);
+  put(&depth, 4);
+  put(&nmain, 4);
+  put(main_offsets, (size_t)nmain * 12);
+  put(&nphase, 4);
+  int total = 0;
+  for (int p = 0; p < nphase; ++p) total += noffs[p];
+  put(values, (size_t)nphase * 4);
+  put(noffs, (size_t)nphase * 4);
+  if (total) put(offsets, (size_t)total * 12);
+  auto hit = m->local_cache.find(ck);
+  if (hit != m->local_cache.end()) {
+    *ok = hit->second;
+    return 0;
+  }
+  const int64_t* n = m->ext;
+  auto inside = [n](const int64_t* c) { return c[0] >= 0 && c[0] < n[0] && c[1] >= 0 && c[1] < n[1] && c[2] >= 0 && c[2] < n[2]; };
+  int result = 1;
+  // (1) mask-0 cells read inside the grid; only cells within the reach of an edge can fail
+  int32_t reach[3] = {0, 0, 0};
+  for (int k = 0; k < nmain; ++k)
+    for (int a = 0; a < 3; ++a) reach[a] = std::max(reach[a], std::abs(main_offsets[3 * k + a]));
+  for (int64_t z = 0; z < n[0] && result; ++z)
+    for (int64_t y = 0; y < n[1] && result; ++y) {
+      const bool band = z < reach[0] || z >= n[0] - reach[0] || y < reach[1] || y >= n[1] - reach[1];
+      for (int64_t x = 0; x < n[2] && result; x = (band || x >= n[2] - reach[2] || x + 1 < reach[2]) ? x + 1
+                                                                                                 : n[2] - reach[2]) {
+        if (m->host[(z * n[1] + y) * n[2] + x] != 0) continue;
+        for (int k = 0; k < nmain; ++k) {
+          const int64_t c[3] = {z + main_offsets[3 * k], y + main_offsets[3 * k + 1], x + main_offsets[3 * k + 2]};
+          if (!inside(c)) {
+            result = 0;
+            break;
+          }
+        }
+      }
+    }
+  // (2) boundary phases: reads inside the grid, never of their own mask value, and never
+  //     closer to an inner box edge than the cell itself (up to the depth's halo)
+  int base = 0;
+  for (int p = 0; p < nphase && result; base += noffs[p], ++p) {
+    auto cv = m->cells.find(values[p]);
+    if (cv == m->cells.end()) continue;
+    int64_t nt[3];
+    for (int a = 0; a < 3; ++a) nt[a] = (n[a] + core[a] - 1) / core[a];
+    for (int64_t cell : cv->second) {
+      const int64_t co[3] = {cell / (n[1] * n[2]), (cell / n[2]) % n[1], cell % n[2]};
+      int64_t lo[3], hi[3];
+      for (int a = 0; a < 3; ++a) box_range(co[a], core[a], halo[a], nt[a], &lo[a], &hi[a]);
+      for (int k = 0; k < noffs[p] && result; ++k) {
+        const int32_t* o = offsets + 3 * (base + k);
+        const int64_t src[3] = {co[0] + o[0], co[1] + o[1], co[2] + o[2]};
+        if (!inside(src) || m->host[(src[0] * n[1] + src[1]) * n[2] + src[2]] == values[p]) {
+          result = 0;
+          break;
+        }
+        for (int a = 0; a < 3 && result; ++a) {
+          if (o[a] == 0) continue;
+          const int64_t need = (int64_t)depth * shrink[a];
+          const int64_t i0 = a == 0 ? lo[0] : (a == 1 ? lo[1] : lo[2]), i1 = a == 0 ? hi[0] : (a == 1 ? hi[1] : hi[2]);
+          for (int64_t i = i0; i <= i1; ++i) {
+            const int64_t dc = inner_distance(co[a], i, core[a], halo[a], n[a]);
+            const int64_t ds = inner_distance(src[a], i, core[a], halo[a], n[a]);
+            if (ds < std::min(dc, need)) {
+              result = 0;
+              break;
+            }
+          }
+        }
       }
       if (!result) break;
     }

@@ -38,6 +38,33 @@ from .types import Floating
 
 B = ir.BinaryOperator
 
+# Work area of a loop in the grid's ``aux`` buffer (xg_mx_layout in xgrid_gen.cuh):
+# FP32 residual, two FP32-sized defect buffers, a 16-bit residual copy (rows
+# padded to AUX_PITCH elements, each part 256-byte aligned), then AUX_SLOT_BYTES
+# of per-launch maxima and an error word.
+AUX_PITCH = 32
+AUX_SLOT_BYTES = 65536
+AUX_BYTES_PER_CELL = 14
+
+
+def aux_bytes(shape) -> int:
+    """Bytes of the work area of a grid of ``shape``."""
+    dims = [int(v) for v in shape]
+    rest = 1
+    for v in dims[:-1]:
+        rest *= v
+    xp = -(-dims[-1] // AUX_PITCH) * AUX_PITCH
+    cells = rest * xp
+
+    def a(v):
+        return (v + 255) // 256 * 256
+    return 3 * a(cells * 4) + a(cells * 2) + AUX_SLOT_BYTES
+
+
+def aux_error_offset(shape) -> int:
+    """Byte offset of the error word (nonzero after a staging copy timed out)."""
+    return aux_bytes(shape) - 4
+
 
 @dataclasses.dataclass(eq=False)
 class MixedPlan:
@@ -219,18 +246,33 @@ class MixedLoopEmitter:
         g = plan.group
         P0 = b.bname((slot, 0, 0))
         S = b.bname((slot, 0, 1))
-        b.emit_fused(tag="res", extra_params=["float* mx_r", "float* mx_d"], extra_args=", float* mx_r, float* mx_d",
-                     extra_fill=["  p.mx_r = mx_r; p.mx_d = mx_d;"],
-                     final=[f"const float rr = (float)({S}[c] - {P0}[c]);", "p.mx_r[c] = rr;", "p.mx_d[c] = rr;"],
+        # residual launch: r = G(P) - P in FP32 (row pitch X + mx_pad), optionally also as the
+        # first defect, and its largest magnitude folded into *mx_max
+        b.emit_fused(tag="res", extra_params=["float* mx_r", "float* mx_d", "int64_t mx_pad", "float* mx_max"],
+                     extra_args=", float* mx_r, float* mx_d, int64_t mx_pad, float* mx_max",
+                     extra_fill=["  p.mx_r = mx_r; p.mx_d = mx_d; p.mx_pad = mx_pad; p.mx_max = mx_max;"],
+                     final=(["float xg_amax = 0.f;"],
+                            [f"const float rr = (float)({S}[c] - {P0}[c]);",
+                             "const I xa = c + ((I)z * (I)p.Y + (I)y) * (I)p.mx_pad;",
+                             "p.mx_r[xa] = rr;",
+                             "if (p.mx_d) p.mx_d[xa] = rr;",
+                             "xg_amax = fmaxf(xg_amax, fabsf(rr));"],
+                            ["if (p.mx_max) xg_block_max_atomic(xg_amax, p.mx_max);"]),
                      swap=False)
+        from .mixed_tb import TemporalDefect
+        self.tb = TemporalDefect(self)
+        tb_device = self.tb.device() if self.tb.usable else []
         defect = self.defect_kernel()
         cs = [f"struct xgm_{n}_{gid} {{"] + [f"  float {name};" for name, _, _ in self.coefs]
         if not self.coefs:
             cs.append("  char xg_empty;")
         cs.append("};")
         gen.device_chunks.append("\n".join(cs))
+        gen.device_chunks.extend(tb_device)
         gen.device_chunks.extend(defect)
         gen.device_chunks.extend(self.correction_kernel())
+        if self.tb.usable:
+            gen.host_chunks.append(self.tb.host())
         gen.host_chunks.append(self.host_functions())
         # host block in the kernel body
         v = plan.loop.variable.name
@@ -344,13 +386,20 @@ class MixedLoopEmitter:
         sweeps = plan.group.sweeps
         bnds = list(range(1, len(sweeps)))
         bsweeps = [sweeps[j] for j in bnds]
+        from .mixed_tb import DSCALE
         P = b.bname((slot, 0, 1))  # boundary phases address the target as version 1
-        extra = ["const float* mx_d"] + [x for j in bnds for x in (f"const int32_t* bo{j}", f"const int64_t* bc{j}")]
+        extra = ["const void* mx_d", "int mx_kind", "const float* mx_slot", "int64_t mx_pad"] + \
+            [x for j in bnds for x in (f"const int32_t* bo{j}", f"const int64_t* bc{j}")]
         params = b.params_struct("mxc", bsweeps or [sweeps[0]], extra)
         K = [f"template <typename I> __global__ void __launch_bounds__(256, 6) xgk_{n}_{gid}_mxc("
              f"const __grid_constant__ struct xgp_{n}_{gid}_mxc p) {{"] + TILE_PROLOGUE + b.restrict_locals(bsweeps or [sweeps[0]]) + \
-            ["  const float* __restrict__ mx_d = p.mx_d;"] + CELL_LOOP + [
-             f"      {P}[c] = {P}[c] + (double)mx_d[c];", "    }}"]
+            [f"  const float xg_inv = p.mx_slot ? xg_pow2f(-xg_scale_exp(*p.mx_slot, {DSCALE})) : 1.f;"] + \
+            CELL_LOOP + [
+             "      const I xa = c + ((I)z * (I)p.Y + (I)y) * (I)p.mx_pad;",
+             "      const float dv = p.mx_kind == 0 ? ((const float*)p.mx_d)[xa] : (p.mx_kind == 1 ? "
+             "__half2float(((const __half*)p.mx_d)[xa]) : __bfloat162float(((const __nv_bfloat16*)p.mx_d)[xa])) "
+             "* xg_inv;",
+             f"      {P}[c] = {P}[c] + (double)dv;", "    }}"]
         for j in bnds:
             s = sweeps[j]
             pre, val = b.value_code(s, False, "    ")
@@ -375,9 +424,8 @@ class MixedLoopEmitter:
         # run-time applicability (same conditions as the fused launch)
         L += [f"static int xgm_{n}_{gid}_ready(xg_grid* G) {{",
               f"  if (!xg_fuse_{n} || !G[{slot}].scratch || !G[{slot}].aux) return 0;",
-              f"  xg_ext e = xg_extent(&G[{slot}]);",
-              "  const int64_t N = e.z * e.y * e.x;",
-              f"  if (G[{slot}].aux_bytes < 3 * N * (int64_t)sizeof(float)) return 0;",
+              "  xg_mx_aux A;",
+              f"  if (xg_mx_layout(&G[{slot}], &A) != 0) return 0;",
               f"  const int32_t* tl = xg_tiling_{n}[{gid}];"]
         for j, offs in plan.group.local_checks:
             flat = ", ".join(str(v) for o in offs for v in o)
@@ -415,12 +463,11 @@ class MixedLoopEmitter:
         # FP64 correction (+ boundary phases)
         bsweeps = [sweeps[j] for j in bnds] or [sweeps[0]]
         P = b.bname((slot, 0, 1))
-        L += [f"static int xgm_{n}_{gid}_correct(xg_grid* G, const struct xgh_{n}_{gid}* h, const float* d, "
-              f"int64_t N, cudaStream_t s) {{",
-              "  (void)N;"]
+        L += [f"static int xgm_{n}_{gid}_correct(xg_grid* G, const struct xgh_{n}_{gid}* h, const void* d, "
+              f"int kind, const float* slot, int64_t pad, cudaStream_t s) {{"]
         L += b.fill_params("mxc", bsweeps, slot)
         L += [f"  p.{P} = (double*)G[{slot}].level[0];",
-              "  p.mx_d = d;",
+              "  p.mx_d = d; p.mx_kind = kind; p.mx_slot = slot; p.mx_pad = pad;",
               "  int64_t ntiles = 0;",
               f"  XG_TRY(xg_mask_tiles(G[{slot}].mask, tl, 0, NULL, NULL, NULL, &ntiles));"]
         for j in bnds:
@@ -435,26 +482,52 @@ class MixedLoopEmitter:
               f"  xg_prof_end({gid * 64 + 60}, s);",
               "  return 0;", "}"]
         # driver
+        tb = self.tb.usable
+        kind, scaled = self.tb.kind, int(self.tb.scaled)
         L += [f"static int xgm_{n}_{gid}_run(xg_grid* G, const struct xgh_{n}_{gid}* h, "
               f"const struct xgm_{n}_{gid}* hm, int64_t K, cudaStream_t s) {{",
-              f"  xg_ext e = xg_extent(&G[{slot}]);",
-              "  const int64_t N = e.z * e.y * e.x;",
-              f"  float* d0 = (float*)G[{slot}].aux;",
-              "  float* d1 = d0 + N;",
-              "  float* r = d1 + N;",
-              f"  int64_t m = xg_mixed_every_{n} > 0 ? xg_mixed_every_{n} : K;",
+              f"  const xg_ext e = xg_extent(&G[{slot}]);",
+              "  xg_mx_aux A;",
+              f"  XG_TRY(xg_mx_layout(&G[{slot}], &A));",
+              f"  const int64_t m = xg_mixed_every_{n} > 0 ? xg_mixed_every_{n} : K;",
+              "  int T = 0, RS = 0;",
+              "  int32_t core[3] = {1, 1, 1}, halo[3] = {0, 0, 0};",
+              f"  const int tb = {f'xgm_{n}_{gid}_tb_plan(G, &T, &RS, core, halo)' if tb else '0'};",
+              "  if (tb < 0) return tb;",
               "  for (int64_t done = 0; done < K;) {",
               "    const int64_t cnt = (K - done) < m ? (K - done) : m;",
-              f"    int rc = xgl_{n}_{gid}_res(G, h, s, r, d0);",
-              "    if (rc < 0) return rc;",
-              "    if (rc == 0) XG_FAIL(\"mixed-precision residual launch is not applicable\");",
-              "    float* din = d0;",
-              "    float* dout = d1;",
-              "    for (int64_t i = 1; i < cnt; ++i) {",
-              f"      XG_TRY(xgm_{n}_{gid}_defect(G, hm, din, dout, r, s));",
-              "      float* t_ = din; din = dout; dout = t_;",
+              "    const int64_t it = cnt - 1;  // defect iterations after the residual",
+              "    const int64_t nl = (tb && it > 0) ? (it + T - 1) / T : 0;"]
+        if tb:
+            L += ["    if (nl > 0 && nl + 2 <= A.nslots) {",
+                  "      // temporally blocked: nl launches of at most T iterations, TMA-staged boxes",
+                  f"      if ({scaled}) XG_CUDA(cudaMemsetAsync(A.slots, 0, (size_t)(nl + 1) * sizeof(float), s));",
+                  f"      int rc = xgl_{n}_{gid}_res(G, h, s, A.r32, NULL, A.XP - e.x, {scaled} ? A.slots : NULL);",
+                  "      if (rc < 0) return rc;",
+                  "      if (rc == 0) XG_FAIL(\"mixed-precision residual launch is not applicable\");",
+                  "      for (int64_t i = 0; i < nl; ++i) {",
+                  "        const int dep = (int)(it / nl + (i < it % nl ? 1 : 0));",
+                  "        void* dout = (i & 1) ? A.dB : A.dA;",
+                  "        const void* din = (i & 1) ? A.dA : A.dB;",
+                  f"        XG_TRY(xgm_{n}_{gid}_tbl(G, hm, &A, dep, RS, core, halo, i == 0, (int)i, din, dout, s));",
+                  "      }",
+                  f"      XG_TRY(xgm_{n}_{gid}_correct(G, h, ((nl - 1) & 1) ? A.dB : A.dA, {kind}, "
+                  f"{scaled} ? A.slots + (nl - 1) : NULL, A.XP - e.x, s));",
+                  "    } else {"]
+        else:
+            L += ["    (void)nl; (void)T; (void)RS; (void)core; (void)halo;", "    {"]
+        L += ["      // one FP32 iteration per launch (dense layout)",
+              f"      int rc = xgl_{n}_{gid}_res(G, h, s, A.r32, (float*)A.dA, 0, NULL);",
+              "      if (rc < 0) return rc;",
+              "      if (rc == 0) XG_FAIL(\"mixed-precision residual launch is not applicable\");",
+              "      float* din = (float*)A.dA;",
+              "      float* dout = (float*)A.dB;",
+              "      for (int64_t i = 1; i < cnt; ++i) {",
+              f"        XG_TRY(xgm_{n}_{gid}_defect(G, hm, din, dout, A.r32, s));",
+              "        float* t_ = din; din = dout; dout = t_;",
+              "      }",
+              f"      XG_TRY(xgm_{n}_{gid}_correct(G, h, din, 0, NULL, 0, s));",
               "    }",
-              f"    XG_TRY(xgm_{n}_{gid}_correct(G, h, din, N, s));",
               "    done += cnt;",
               "  }",
               "  return 0;", "}"]

@@ -1,0 +1,326 @@
+"""Temporally blocked defect iterations of a mixed-precision loop (2-D grids).
+
+The defect iteration ``d <- L(d) + r`` of ``xgrid_gb300.mixed`` runs ``T``
+iterations per launch instead of one.  Each CTA owns a tile of ``TY x TX``
+cells and works on a *box*: the tile plus a halo of ``HY = T * sy`` rows and
+``HX = roundup(T * sx, 8)`` columns per side (``sy, sx``: reach of the loop
+body's main sweep).  Per launch:
+
+1. one thread stages the box of ``d`` and of ``r`` into shared memory with two
+   TMA loads (``cp.async.bulk.tensor.2d``, completion on an mbarrier); cells
+   outside the grid read as zero;
+2. every thread takes a column strip of ``RS`` rows of the box into registers
+   (block of 128 x 2 threads, box of 128 x 2*RS cells); vertical neighbours come
+   from the thread's own registers, horizontal and strip-edge neighbours from a
+   shared copy of the current iterate (two buffers, one barrier per iteration);
+3. boxes that contain boundary cells run the loop body's phases in order: the
+   main sweep on mask-0 cells, each ``with boundary(k)`` phase on its cells of
+   the box (per-tile lists of box-local indices), then ``+ r``;
+4. the tile's cells are written back (FP32, or 16-bit with a power-of-two scale
+   per field and launch).
+
+Cells at distance ``< k * s`` from an inner box edge are stale after ``k``
+iterations; the halo keeps the tile itself exact.  ``xg_mask_box_check`` (run
+time, per mask and tiling) proves that the boundary phases never read a stale
+cell; when it fails the loop falls back to one iteration per launch.  The FP32
+variant performs the same FP32 operations per cell as the one-iteration kernel,
+so both give the same bits.
+"""
+from __future__ import annotations
+
+from . import analysis
+
+BX = 128          # box columns = threads along x
+STRIPS = 2        # thread rows; the box has STRIPS * RS rows
+ROWS = (8, 16, 24)
+DSCALE = 8        # defect: an input of largest magnitude m is stored as m * 2^s in [2^8, 2^9)
+RSCALE = 14       # residual (fixed over the loop): [2^14, 2^15), below the FP16 maximum
+STORAGE = {"fp32": ("float", 0, "CU_TENSOR_MAP_DATA_TYPE_FLOAT32"),
+           "fp16": ("__half", 1, "CU_TENSOR_MAP_DATA_TYPE_FLOAT16"),
+           "bf16": ("__nv_bfloat16", 2, "CU_TENSOR_MAP_DATA_TYPE_BFLOAT16")}
+
+
+def target_offsets(sweep, slot: int) -> list:
+    """Distinct (z, y, x) offsets of the target's time-0 loads in a sweep."""
+    out = []
+    for _, ld in sweep.loads:
+        if ld.slot == slot and ld.level == 0 and ld.version in (0, 1):
+            o = tuple(analysis.pad3(ld.offset))
+            if o not in out:
+                out.append(o)
+    return out
+
+
+class TemporalDefect:
+    """Kernel and host launcher of the temporally blocked defect iterations."""
+
+    def __init__(self, mx) -> None:
+        from .mixed import LinearEmitter
+        self.mx = mx
+        self.LinearEmitter = LinearEmitter
+        gen, plan = mx.gen, mx.plan
+        self.gen = gen
+        self.n, self.gid = gen.op.name, mx.gid
+        self.slot = plan.slot
+        self.target = plan.target
+        self.sweeps = plan.group.sweeps
+        self.bnds = list(range(1, len(self.sweeps)))
+        self.dim = gen.defn.scope[plan.target].type.dimension
+        self.dt, self.kind, self.cutype = STORAGE[gen.cfg.mixed]
+        self.scaled = self.kind != 0
+        self.main_offs = target_offsets(self.sweeps[0], self.slot)
+        self.sy = max([abs(o[1]) for o in self.main_offs] + [0])
+        self.sx = max([abs(o[2]) for o in self.main_offs] + [0])
+        self.usable = self.dim == 2 and all(o[0] == 0 for o in self.main_offs)
+
+    # ----------------------------------------------------------- device code
+    def _lin(self, sweep, load) -> str:
+        code = self.LinearEmitter(self.mx, self.target, load).lin(sweep.stmt.value)
+        return "0.0f" if code is None else code
+
+    def _strip_loader(self, buf: str):
+        """Load of the defect at a stencil offset for row i of the thread's strip."""
+        def load(st):
+            oz, oy, ox = analysis.pad3(st.space_offset)
+            cx = "lx" if ox == 0 else f"cx_{'m' if ox < 0 else 'p'}{abs(ox)}"
+            smem = f"{buf}[xg_clampi(ly0 + i + ({oy}), 0, BY - 1) * BX + {cx}]"
+            if ox == 0 and oy == 0:
+                return "d[i]"
+            if ox == 0:
+                return f"((i + ({oy}) >= 0 && i + ({oy}) < RS) ? d[xg_clampi(i + ({oy}), 0, RS - 1)] : {smem})"
+            return smem
+        return load
+
+    @staticmethod
+    def _box_loader(buf: str):
+        def load(st):
+            oz, oy, ox = analysis.pad3(st.space_offset)
+            return f"{buf}[xg_clampi(c + ({oy}) * BX + ({ox}), 0, BY * BX - 1)]"
+        return load
+
+    def device(self) -> list:
+        n, gid, dt = self.n, self.gid, self.dt
+        main = self.sweeps[0]
+        xs = sorted({o[2] for o in self.main_offs if o[2]})
+        P = [f"struct xgp_{n}_{gid}_mxt {{",
+             "  CUtensorMap md;  // defect in (storage type), box 128 x BY",
+             "  CUtensorMap mr;  // residual (FP32 on the first launch and in FP32 mode, else storage type)",
+             f"  struct xgm_{n}_{gid} k;",
+             "  int Y, X, XP, TY, TX, HY, HX, nty, ntx, dep, first, li;",
+             "  void* dout;",
+             "  void* rout;",
+             "  float* sl;",
+             "  int* err;",
+             "  const int32_t* m0;",
+             "  const uint8_t* bzero;"]
+        for j in self.bnds:
+            P += [f"  const int32_t* bo{j};", f"  const int32_t* bl{j};"]
+        P.append("};")
+        K = [f"template <typename Dt, int RS>",
+             f"__global__ void __launch_bounds__(256, 2) xgk_{n}_{gid}_mxt(const __grid_constant__ "
+             f"struct xgp_{n}_{gid}_mxt p) {{",
+             "  constexpr int BX = 128, BY = 2 * RS;",
+             "  constexpr bool scaled = sizeof(Dt) == 2;",
+             "  extern __shared__ unsigned char xg_dsm[];",
+             "  __shared__ __align__(8) uint64_t xg_bar;",
+             "  float* sA = (float*)(((uintptr_t)xg_dsm + 1023) & ~(uintptr_t)1023);",
+             "  float* sB = sA + BY * BX;",
+             "  const int lx = threadIdx.x, tid = lx + BX * (int)threadIdx.y, ly0 = (int)threadIdx.y * RS;",
+             "  const int t = blockIdx.x;",
+             "  const int ity = t / p.ntx, itx = t - ity * p.ntx;",
+             "  const int by = ity * p.TY - p.HY, bx = itx * p.TX - p.HX;",
+             "  // stage the boxes of r and (after the first launch) d with TMA",
+             "  if (tid == 0) xg_mbar_init(&xg_bar, 1);",
+             "  __syncthreads();",
+             "  if (tid == 0) {",
+             "    const unsigned rb = (p.first || !scaled) ? 4u : (unsigned)sizeof(Dt);",
+             "    xg_mbar_expect_tx(&xg_bar, (unsigned)(BY * BX) * (rb + (p.first ? 0u : (unsigned)sizeof(Dt))));",
+             "    xg_tma_load_2d(sB, &p.mr, bx, by, &xg_bar);",
+             "    if (!p.first) xg_tma_load_2d(sA, &p.md, bx, by, &xg_bar);",
+             "  }",
+             "  const bool landed = xg_mbar_wait(&xg_bar, 0, XG_WAIT_LIMIT);",
+             "  if (__syncthreads_or(!landed)) {  // the copy did not complete: report, let it drain, stop",
+             "    if (tid == 0) {",
+             "      atomicExch(p.err, 1);",
+             "      xg_mbar_wait(&xg_bar, 0, XG_WAIT_LIMIT);",
+             "    }",
+             "    return;",
+             "  }",
+             "  float d[RS], rr[RS];",
+             "  {",
+             f"    const float ir = (scaled && !p.first) ? xg_pow2f(-xg_scale_exp(p.sl[0], {RSCALE})) : 1.f;",
+             f"    const float id = (scaled && !p.first) ? xg_pow2f(-xg_scale_exp(p.sl[p.li - 1], {DSCALE})) : 1.f;",
+             "    const Dt* __restrict__ hA = (const Dt*)sA;",
+             "    const Dt* __restrict__ hB = (const Dt*)sB;",
+             "#pragma unroll",
+             "    for (int i = 0; i < RS; ++i) {",
+             "      const int c = (ly0 + i) * BX + lx;",
+             "      rr[i] = (p.first || !scaled) ? sB[c] : xg_from_store(hB[c]) * ir;",
+             "      d[i] = p.first ? rr[i] : xg_from_store(hA[c]) * id;",
+             "    }",
+             "  }",
+             "  __syncthreads();"]
+        for o in xs:
+            nm = f"cx_{'m' if o < 0 else 'p'}{abs(o)}"
+            K.append(f"  const int {nm} = xg_clampi(lx + ({o}), 0, BX - 1);")
+        K += ["  if (p.bzero[t]) {  // no boundary cell in the box: one pass per iteration",
+              "    for (int k = 0; k < p.dep; ++k) {",
+              "      float* __restrict__ cur = (k & 1) ? sB : sA;",
+              "#pragma unroll",
+              "      for (int i = 0; i < RS; ++i) cur[(ly0 + i) * BX + lx] = d[i];",
+              "      __syncthreads();",
+              "      float nd[RS];",
+              "#pragma unroll",
+              f"      for (int i = 0; i < RS; ++i) nd[i] = {self._lin(main, self._strip_loader('cur'))} + rr[i];",
+              "#pragma unroll",
+              "      for (int i = 0; i < RS; ++i) d[i] = nd[i];",
+              "    }",
+              "  } else {  // main sweep on mask-0 cells, boundary phases in program order, then + r",
+              "    unsigned mz = 0;",
+              "    {",
+              "      const int gx = bx + lx;",
+              "#pragma unroll",
+              "      for (int i = 0; i < RS; ++i) {",
+              "        const int gy = by + ly0 + i;",
+              "        if (gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X && p.m0[(int64_t)gy * p.X + gx] == 0) "
+              "mz |= 1u << i;",
+              "      }",
+              "    }",
+              "    for (int k = 0; k < p.dep; ++k) {",
+              "#pragma unroll",
+              "      for (int i = 0; i < RS; ++i) sA[(ly0 + i) * BX + lx] = d[i];",
+              "      __syncthreads();",
+              "      float nd[RS];",
+              "#pragma unroll",
+              f"      for (int i = 0; i < RS; ++i) nd[i] = ((mz >> i) & 1u) ? "
+              f"{self._lin(main, self._strip_loader('sA'))} : d[i];",
+              "#pragma unroll",
+              "      for (int i = 0; i < RS; ++i) sB[(ly0 + i) * BX + lx] = nd[i];",
+              "      __syncthreads();"]
+        for j in self.bnds:
+            K += [f"      for (int e = p.bo{j}[t] + tid; e < p.bo{j}[t + 1]; e += 2 * BX) {{",
+                  f"        const int c = p.bl{j}[e];",
+                  f"        sB[c] = {self._lin(self.sweeps[j], self._box_loader('sB'))};",
+                  "      }",
+                  "      __syncthreads();"]
+        K += ["#pragma unroll",
+              "      for (int i = 0; i < RS; ++i) d[i] = sB[(ly0 + i) * BX + lx] + rr[i];",
+              "    }",
+              "  }",
+              "  // the tile's own cells go back to global memory",
+              f"  const float os = scaled ? xg_pow2f(xg_scale_exp(p.sl[p.li], {DSCALE})) : 1.f;",
+              f"  const float rs = scaled ? xg_pow2f(xg_scale_exp(p.sl[0], {RSCALE})) : 1.f;",
+              "  Dt* __restrict__ dout = (Dt*)p.dout;",
+              "  Dt* __restrict__ rout = (Dt*)p.rout;",
+              "  const int gx = bx + lx;",
+              "  const bool col = lx >= p.HX && lx < p.HX + p.TX && gx < p.X;",
+              "  float amax = 0.f;",
+              "#pragma unroll",
+              "  for (int i = 0; i < RS; ++i) {",
+              "    const int ly = ly0 + i, gy = by + ly;",
+              "    if (col && ly >= p.HY && ly < p.HY + p.TY && gy < p.Y) {",
+              "      const int64_t a = (int64_t)gy * p.XP + gx;",
+              "      dout[a] = xg_to_store<Dt>(d[i] * os);",
+              "      if (scaled && rout) rout[a] = xg_to_store<Dt>(rr[i] * rs);",
+              "      amax = fmaxf(amax, fabsf(d[i]));",
+              "    }",
+              "  }",
+              "  if (scaled) xg_block_max_atomic(amax, p.sl + p.li + 1);",
+              "}"]
+        return ["\n".join(P), "\n".join(K)]
+
+    # ------------------------------------------------------------- host code
+    def host(self) -> str:
+        n, gid, slot, dt = self.n, self.gid, self.slot, self.dt
+        cfg = self.gen.cfg
+        mo = [v for o in self.main_offs for v in o]
+        vals, nof, offs = [], [], []
+        for j in self.bnds:
+            s = self.sweeps[j]
+            os_ = target_offsets(s, self.slot)
+            vals.append(s.mask)
+            nof.append(len(os_))
+            offs += [v for o in os_ for v in o]
+
+        def arr(name, values):
+            if not values:
+                return [f"  const int32_t* {name} = NULL;"]
+            return [f"  static const int32_t {name}[] = {{{', '.join(str(v) for v in values)}}};"]
+
+        L = [f"static int32_t xg_mxt_{n}[2] = {{{int(cfg.mixed_temporal)}, {int(cfg.mixed_rows)}}};",
+             f'extern "C" int xg_mixed_tb_{n}(int depth, int rows) {{',
+             "  if (depth < 0 || depth > 16) XG_FAIL(\"temporal blocking: depth %d outside 0..16\", depth);",
+             "  if (rows >= 0 && rows != 8 && rows != 16 && rows != 24) "
+             "XG_FAIL(\"temporal blocking: rows per thread must be 8, 16 or 24, not %d\", rows);",
+             f"  xg_mxt_{n}[0] = depth;",
+             f"  if (rows >= 0) xg_mxt_{n}[1] = rows;",
+             "  return 0;",
+             "}",
+             f"// temporal blocking of the defect iterations: box geometry for this grid, 1 when usable",
+             f"static int xgm_{n}_{gid}_tb_plan(xg_grid* G, int* T, int* RS, int32_t* core, int32_t* halo) {{",
+             f"  const xg_grid* g = &G[{slot}];",
+             f"  if (g->ndim != 2 || xg_mxt_{n}[0] < 1 || !g->mask) return 0;",
+             f"  *T = xg_mxt_{n}[0];",
+             f"  *RS = xg_mxt_{n}[1];",
+             "  if (*RS != 8 && *RS != 16 && *RS != 24) return 0;",
+             f"  halo[0] = 0; halo[1] = *T * {self.sy}; halo[2] = (*T * {self.sx} + 7) / 8 * 8;",
+             "  core[0] = 1; core[1] = 2 * *RS - 2 * halo[1]; core[2] = 128 - 2 * halo[2];",
+             "  if (core[1] < 1 || core[2] < 8) return 0;",
+             f"  const int32_t shrink[3] = {{0, {self.sy}, {self.sx}}};"]
+        L += arr("mo", mo) + arr("vals", vals) + arr("nof", nof) + arr("offs", offs)
+        L += ["  int ok = 0;",
+              f"  XG_TRY(xg_mask_box_check(g->mask, core, halo, shrink, *T, {len(self.main_offs)}, mo, "
+              f"{len(vals)}, vals, nof, offs, &ok));",
+              "  return ok;",
+              "}",
+              f"template <int RS>",
+              f"static int xgm_{n}_{gid}_go(const struct xgp_{n}_{gid}_mxt& p, int64_t nt, cudaStream_t s) {{",
+              "  static int avail = -1;",
+              f"  if (avail < 0) XG_TRY(xg_smem_optin(xgk_{n}_{gid}_mxt<{dt}, RS>, &avail));",
+              "  const size_t smem = (size_t)2 * (2 * RS) * 128 * sizeof(float) + 1024;",
+              "  if (smem > (size_t)avail) XG_FAIL(\"temporal blocking: %zu bytes of shared memory, %d available\", "
+              "smem, avail);",
+              f"  xgk_{n}_{gid}_mxt<{dt}, RS><<<(unsigned)nt, dim3(128, 2, 1), smem, s>>>(p);",
+              "  XG_CUDA(cudaGetLastError());",
+              "  return 0;",
+              "}",
+              f"static int xgm_{n}_{gid}_tbl(xg_grid* G, const struct xgm_{n}_{gid}* hm, const xg_mx_aux* A, "
+              f"int dep, int RS, const int32_t* core, const int32_t* halo, int first, int li, const void* din, "
+              f"void* dout, cudaStream_t s) {{",
+              f"  struct xgp_{n}_{gid}_mxt p;",
+              "  memset(&p, 0, sizeof p);",
+              "  p.k = *hm;",
+              f"  const xg_ext e = xg_extent(&G[{slot}]);",
+              "  p.Y = (int)e.y; p.X = (int)e.x; p.XP = (int)A->XP;",
+              "  p.TY = core[1]; p.TX = core[2]; p.HY = halo[1]; p.HX = halo[2];",
+              "  p.nty = (p.Y + p.TY - 1) / p.TY; p.ntx = (p.X + p.TX - 1) / p.TX;",
+              "  p.dep = dep; p.first = first; p.li = li;",
+              "  const int BY = 2 * RS;",
+              f"  const int es = (int)sizeof({dt});",
+              f"  if (!first) XG_TRY(xg_tmap_2d(&p.md, din, {self.cutype}, es, e.x, e.y, A->XP * es, 128, BY));",
+              f"  if (first || !{int(self.scaled)})",
+              "    XG_TRY(xg_tmap_2d(&p.mr, A->r32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, e.x, e.y, A->XP * 4, 128, BY));",
+              "  else",
+              f"    XG_TRY(xg_tmap_2d(&p.mr, A->r16, {self.cutype}, es, e.x, e.y, A->XP * es, 128, BY));",
+              "  p.dout = dout;",
+              f"  p.rout = (first && {int(self.scaled)}) ? A->r16 : NULL;",
+              "  p.sl = A->slots;",
+              "  p.err = A->err;",
+              f"  p.m0 = xg_mask_device(G[{slot}].mask);",
+              "  int64_t nt = 0;",
+              f"  XG_TRY(xg_mask_boxes(G[{slot}].mask, core, halo, 0, &p.bzero, NULL, NULL, &nt));"]
+        for j in self.bnds:
+            L.append(f"  XG_TRY(xg_mask_boxes(G[{slot}].mask, core, halo, {self.sweeps[j].mask}, NULL, &p.bo{j}, "
+                     f"&p.bl{j}, &nt));")
+        L += ["  if (nt != (int64_t)p.nty * p.ntx) XG_FAIL(\"box table mismatch\");",
+              f"  xg_prof_launch({gid * 64 + 59}, s);",
+              "  switch (RS) {",
+              f"    case 8: XG_TRY(xgm_{n}_{gid}_go<8>(p, nt, s)); break;",
+              f"    case 16: XG_TRY(xgm_{n}_{gid}_go<16>(p, nt, s)); break;",
+              f"    case 24: XG_TRY(xgm_{n}_{gid}_go<24>(p, nt, s)); break;",
+              "    default: XG_FAIL(\"temporal blocking: %d rows per thread is not compiled\", RS);",
+              "  }",
+              f"  xg_prof_end({gid * 64 + 59}, s);",
+              "  return 0;",
+              "}"]
+        return "\n".join(L)

@@ -13,7 +13,7 @@ import ctypes
 
 import numpy as np
 
-from . import device, runtime
+from . import device, mixed, runtime
 from .codegen import CudaGenerator
 from .compiler import Compiler, Library
 from .config import get_config
@@ -48,6 +48,18 @@ class NativeKernel:
         if self.mixed_fn is not None:
             self.mixed_fn.argtypes = [ctypes.c_int64]
             self.mixed_fn.restype = ctypes.c_int
+
+    def set_mixed_temporal(self, depth: int, rows: int | None = None) -> None:
+        """Defect iterations per launch of mixed-precision loops (0: one FP32
+        iteration per launch, no shared-memory staging) and rows per thread of
+        the temporally blocked kernel (8, 16 or 24)."""
+        fn = getattr(self.lib.dylib, f"xg_mixed_tb_{self.module.name}", None)
+        if fn is None:
+            self.logger.dead(f"kernel '{self.module.name}' has no temporally blocked mixed-precision loop")
+        fn.restype = ctypes.c_int
+        if fn(ctypes.c_int(int(depth)), ctypes.c_int(int(rows) if rows is not None else -1)) != 0:
+            self.logger.dead(runtime.last_error())
+        runtime.load().xg_graph_clear(self.fn_ptr)
 
     def set_mixed_every(self, every: int) -> None:
         """Iterations between FP64 corrections of mixed-precision loops (0 = once per loop)."""
@@ -94,7 +106,7 @@ class NativeKernel:
             g._op_invoke(self.depth, self.op.tick)
         uploaded = False
         for i, g in enumerate(grids):
-            aux = self.module.aux_per_cell.get(i, 0) * int(np.prod(g.shape))
+            aux = mixed.aux_bytes(g.shape) if i in self.module.aux_per_cell else 0
             uploaded |= g._sync_device(i in self.scratch_slots, aux)
         if uploaded:
             device.stream().synchronize()

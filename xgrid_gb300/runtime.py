@@ -50,6 +50,14 @@ SIGNATURES = {
     "xg_mask_tile_local": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
                                           ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_int)]),
+    "xg_mask_boxes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                     ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                     ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64)]),
+    "xg_mask_box_check": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.c_int32, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int)]),
     "xg_call": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XGGrid), ctypes.c_int, ctypes.c_void_p,
                                ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int]),
     "xg_graph_clear": (ctypes.c_int, [ctypes.c_void_p]),
