@@ -238,6 +238,20 @@ class CudaGenerator:
                 return f"{'pow' if double else 'powf'}({base}, {self.expr(e.right, env)})"
             if e.operator is ir.BinaryOperator.Mod and "int" not in self.ctype(e):
                 self.logger.dead("Operator '%' requires integer operands in C")
+            every = getattr(env, "int_adds", 0)
+            if every and e.operator in (ir.BinaryOperator.Add, ir.BinaryOperator.Sub) and self.ctype(e) == "double":
+                # every n-th distinct FP64 addition of a sweep runs on the integer pipe (same IEEE
+                # result); repeated subexpressions keep one choice so the compiler can still merge them
+                lc, rc = self.expr(e.left, env), self.expr(e.right, env)
+                key = (e.operator.value, lc, rc)
+                soft = env.add_memo.get(key)
+                if soft is None:
+                    env.add_count += 1
+                    soft = env.add_memo[key] = env.add_count % every == 0
+                if soft:
+                    fn = "xg_dadd_i" if e.operator is ir.BinaryOperator.Add else "xg_dsub_i"
+                    return f"{fn}((double)({lc}), (double)({rc}))"
+                return f"({lc} {e.operator.value} {rc})"
             return f"({self.expr(e.left, env)} {e.operator.value} {self.expr(e.right, env)})"
         if isinstance(e, ir.Call):
             return self.call(e, env)
@@ -700,6 +714,9 @@ class SweepEnv:
         self.loadnames = loadnames
         self.div_map = div_map or {}
         self.mul_map = mul_map or {}
+        self.int_adds = int(getattr(gen.cfg, "int_adds", 0))
+        self.add_count = 0
+        self.add_memo: dict = {}
 
     def substitute(self, e):
         h = self.hoisted.get(id(e))

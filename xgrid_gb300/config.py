@@ -28,6 +28,9 @@ Backend options (new keywords, all optional):
   per launch without shared-memory staging (FP32 storage).
 * ``mixed_rows``: rows per thread of that kernel (8, 16 or 24; the tile is
   128 columns by twice this many rows, halo included).
+* ``int_adds``: every n-th FP64 addition or subtraction of a sweep runs as an
+  exact round-to-nearest integer-pipe routine instead of the FP64 unit (0: none,
+  1: all); the results are the same bits, only the pipe balance changes.
 * ``graph``: capture each distinct kernel call into a CUDA graph and replay it.
 * ``fuse``: fuse consecutive sweeps into one launch where the masks allow it.
 * ``divisor``: precompute loop-invariant divisors on the host and divide with a
@@ -70,6 +73,7 @@ class Configuration:
     autotune: bool = True
     mixed_temporal: int = 4
     mixed_rows: int = 16
+    int_adds: int = 0
 
     def __repr__(self) -> str:
         return repr(dataclasses.asdict(self))
@@ -100,7 +104,7 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
          opt_level: Literal[0, 1, 2, 3] = 2, precision: Literal["float", "double"] = "float",
          exact: bool = True, mixed: Optional[str] = None, graph: bool = True,
          fuse: bool = True, divisor: bool = True, mixed_every: int = 0, autotune: bool = True,
-         mixed_temporal: int = 4, mixed_rows: int = 16) -> None:
+         mixed_temporal: int = 4, mixed_rows: int = 16, int_adds: int = 0) -> None:
     """Set the global configuration (same keywords as the reference plus GPU options)."""
     global _config
     if sys.version_info < (3, 10):
@@ -115,9 +119,11 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
         logger.dead(f"Invalid opt_level '{opt_level}'")
     if not 0 <= int(mixed_temporal) <= 16:
         logger.dead(f"Invalid mixed_temporal {mixed_temporal}: 0 (off) to 16 iterations per launch")
+    if int(int_adds) < 0:
+        logger.dead(f"Invalid int_adds {int_adds}: 0 (off) or every n-th addition")
     if int(mixed_rows) not in MIXED_ROWS:
         logger.dead(f"Invalid mixed_rows {mixed_rows}, expected one of {MIXED_ROWS}")
     _config = Configuration(parallel, list(cc), cacheroot, comment, overstep, opt_level,
                             precision, exact, mixed, graph, fuse, divisor, int(mixed_every), bool(autotune),
-                            int(mixed_temporal), int(mixed_rows))
+                            int(mixed_temporal), int(mixed_rows), int(int_adds))
     logger.info(f"initialized with configuration: {_config}")

@@ -460,3 +460,63 @@ static inline int xg_smem_optin(K* kernel, int* avail) {
   if (avail) *avail = dyn;
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Binary64 addition on the integer pipe.
+//
+// GB300 issues FP64 arithmetic at a small fraction of its integer rate, so FP64
+// sweeps are bound by the FP64 pipe.  xg_dadd_i(a, b) returns RN(a + b) (IEEE
+// 754 round to nearest, ties to even) with integer instructions: the larger
+// operand's significand sits at bits 62..10 of a 64-bit word, the smaller one
+// is shifted right by the exponent difference with every bit shifted out
+// OR-ed into bit 0 (sticky), the two are added or subtracted, the sum is
+// normalised back to bits 62..10 and rounded at bit 10.  Ten bits below the
+// last significand bit make the sticky bit irrelevant except to break exact
+// ties, so the rounding is the IEEE one.  Zeros, subnormals, infinities, NaN
+// and sums that leave the normal range take the hardware operation, so the
+// result is RN(a + b) for every input.  Generated sweeps send part of their
+// FP64 additions here so that the FP64 and the integer pipes both work.
+template <bool SUB>
+__device__ __forceinline__ double xg_dadd_core(double a, double b) {
+  const unsigned long long M = 0x7fffffffffffffffull;
+  const unsigned long long A = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long B = (unsigned long long)__double_as_longlong(b) ^ (SUB ? ~M : 0ull);
+  const unsigned long long MA = A & M, MB = B & M;
+  if ((unsigned)(MA >> 52) - 1u > 2045u || (unsigned)(MB >> 52) - 1u > 2045u) {
+    if (MB == 0ull && MA != 0ull) return a;                           // x +- 0 = x
+    if (MA == 0ull && MB != 0ull) return __longlong_as_double((long long)B);  // 0 + y, 0 - y
+    return SUB ? __dsub_rn(a, b) : __dadd_rn(a, b);
+  }
+  const bool sw = MA < MB;
+  const unsigned long long X = sw ? B : A, Y = sw ? A : B;  // X: larger magnitude, its sign is the result's
+  const unsigned long long MX = sw ? MB : MA, MY = sw ? MA : MB;
+  const int ex = (int)(MX >> 52);
+  const int d = ex - (int)(MY >> 52);
+  const unsigned long long F = 0x000fffffffffffffull, H = 0x0010000000000000ull;
+  const unsigned long long mx = ((MX & F) | H) << 10;
+  const unsigned long long my = ((MY & F) | H) << 10;
+  const int k = d < 63 ? d : 63;
+  unsigned long long sy = my >> k;
+  sy |= (unsigned long long)((sy << k) != my);
+  unsigned long long s;
+  int e = ex;
+  if (((X ^ Y) >> 63) == 0ull) {
+    s = mx + sy;  // < 2^64
+    const unsigned long long c = s >> 63;
+    s = (s >> c) | (s & c);
+    e += (int)c;
+  } else {
+    s = mx - sy;
+    if (s == 0ull) return 0.0;  // exact cancellation is +0 under round to nearest
+    const int z = __clzll((long long)s) - 1;
+    s <<= z;
+    e -= z;
+  }
+  if (e < 1 || e > 2046) return SUB ? __dsub_rn(a, b) : __dadd_rn(a, b);
+  s += 0x1ffull + ((s >> 10) & 1ull);
+  const unsigned long long r = ((unsigned long long)(e - 1) << 52) + (s >> 10);  // a carry bumps the exponent
+  return __longlong_as_double((long long)(r | (X & ~M)));
+}
+
+__device__ __forceinline__ double xg_dadd_i(double a, double b) { return xg_dadd_core<false>(a, b); }
+__device__ __forceinline__ double xg_dsub_i(double a, double b) { return xg_dadd_core<true>(a, b); }
