@@ -57,7 +57,10 @@ typedef struct xg_grid {
                                       level[0] by two-phase sweeps (may be NULL)      */
     xg_mask* mask;                 /* boundary mask handle                            */
     void* aux;                     /* device work area of mixed-precision loops
-                                      (defect and residual fields; may be NULL)       */
+                                      (residual, defect and scale fields; may be
+                                      NULL); zero it when allocating: its last 4
+                                      bytes are an error word that a kernel sets to
+                                      1 when a TMA staging copy does not complete    */
     int64_t aux_bytes;             /* size of aux                                     */
 } xg_grid;
 

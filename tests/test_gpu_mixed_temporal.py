@@ -66,7 +66,10 @@ def test_fp32_temporal_equals_one_iteration_per_launch(cacheroot, shape, tempora
     ref, n_ref, _ = run(k, shape, 6, 0)
     out, n_tb, word = run(k, shape, 6, temporal, rows)
     for g in "puv":
-        assert out[g].tobytes() == ref[g].tobytes(), g
+        bad = np.argwhere(out[g] != ref[g])
+        assert bad.size == 0, (f"{g}: {len(bad)} cells differ, first {bad[:6].tolist()}, largest "
+                               f"{np.abs(out[g] - ref[g]).max():.3e} (field max {np.abs(ref[g]).max():.3e}), "
+                               f"staging error word {word}")
     assert word == 0
     # 49 defect launches per step become ceil(49 / temporal)
     assert n_tb < n_ref or temporal == 1

@@ -173,7 +173,8 @@ class Grid:
         if need_scratch and self._scratch is None:
             self._scratch = device.alloc_bytes(self._nbytes)
         if aux_bytes and (self._aux is None or self._aux.numel() < aux_bytes):
-            self._aux = device.alloc_bytes(aux_bytes)
+            # zeroed: the work area ends with an error word that kernels only ever set
+            self._aux = device.alloc_bytes(aux_bytes, zero=True)
         if self._mask_dirty or self._mask is None:
             self._upload_mask()
         return uploaded

@@ -83,7 +83,9 @@ class TemporalDefect:
         def load(st):
             oz, oy, ox = analysis.pad3(st.space_offset)
             cx = "lx" if ox == 0 else f"cx_{'m' if ox < 0 else 'p'}{abs(ox)}"
-            smem = f"{buf}[xg_clampi(ly0 + i + ({oy}), 0, BY - 1) * BX + {cx}]"
+            # rows inside the thread's strip need no clamp (decided at compile time once i is unrolled)
+            row = f"((i + ({oy}) >= 0 && i + ({oy}) < RS) ? ly0 + i + ({oy}) : xg_clampi(ly0 + i + ({oy}), 0, BY - 1))"
+            smem = f"{buf}[{row} * BX + {cx}]"
             if ox == 0 and oy == 0:
                 return "d[i]"
             if ox == 0:
@@ -117,7 +119,7 @@ class TemporalDefect:
             P += [f"  const int32_t* bo{j};", f"  const int32_t* bl{j};"]
         P.append("};")
         K = [f"template <typename Dt, int RS>",
-             f"__global__ void __launch_bounds__(256, 2) xgk_{n}_{gid}_mxt(const __grid_constant__ "
+             f"__global__ void __launch_bounds__(256, RS <= 8 ? 4 : (RS <= 16 ? 3 : 2)) xgk_{n}_{gid}_mxt(const __grid_constant__ "
              f"struct xgp_{n}_{gid}_mxt p) {{",
              "  constexpr int BX = 128, BY = 2 * RS;",
              "  constexpr bool scaled = sizeof(Dt) == 2;",
