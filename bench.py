@@ -73,7 +73,7 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--mixed", default=None, choices=[None, "fp32", "fp16", "bf16"],
                     help="kernels mode: precision lowering of the pressure loop")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "batch"],
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "batch", "adjoint"],
                     help="kernels mode: which workload to run")
     ap.add_argument("--temporal", default=None,
                     help="kernels mode, batch workload: steps per launch, or depth,ty,tx (1 = none)")
@@ -99,6 +99,23 @@ def kernels_only(args) -> None:
             workloads.convdiff2d.batch(probs, args.steps, temporal=temporal)
         device.synchronize()
         print(json.dumps({"mode": "kernels", "workload": "batch", "calls": args.warmup + 1}))
+        return
+    if args.workload == "adjoint":
+        # 3-D variable-coefficient diffusion at n^3 FP32: forward rollout + gradient, checkpoints every 10
+        import torch
+        from xgrid_gb300 import adjoint
+        from xgrid_gb300.operator import Operator
+        xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+                   opt_level=3, overstep="wrap")
+        k = Operator(workloads.diffuse3d.func, "kernel", "diffuse3d")
+        u0, kap, tgt, dt = workloads.adjoint_setup(args.n, 2)
+        u0, kap, tgt = (torch.tensor(x, device="cuda") for x in (u0, kap, tgt))
+        ro = adjoint.Rollout(k, args.steps, 10)
+        for _ in range(args.warmup + 1):
+            a, bb = u0.clone().requires_grad_(True), kap.clone().requires_grad_(True)
+            ((ro(a, {"k": bb}, (dt,)) - tgt) ** 2).mean().backward()
+        device.synchronize()
+        print(json.dumps({"mode": "kernels", "workload": "adjoint", "n": args.n, "calls": args.warmup + 1}))
         return
     xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
                opt_level=3, mixed=args.mixed, mixed_temporal=args.mixed_temporal)

@@ -44,7 +44,7 @@ from .types import (Boolean, Floating, GridType, Ignore, Integer, Pointer, Struc
 OVERSTEP = {"none": "XG_OVERSTEP_NONE", "limit": "XG_OVERSTEP_LIMIT", "wrap": "XG_OVERSTEP_WRAP"}
 
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
-DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 64, 32, 32, 8, 1), 3: (1, 16, 32, 32, 8, 1)}
+DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 64, 32, 32, 8, 1), 3: (32, 8, 32, 32, 8, 1)}
 
 # tile prologue and cell loop shared by the tile kernels (32-bit coordinates,
 # 64-bit linear index per row)
@@ -965,6 +965,8 @@ class SweepGroupEmitter:
         False generic per-grid addressing."""
         b = self.bname((ld.slot, ld.level, ld.version))
         oz, oy, ox = ld.offset
+        if fast == "edge_row":
+            return f"{b}[{self._row_base(oz, oy)} + (I){self.axis_name('x', ox)}]"
         if fast == "edge":
             if self.gen.cfg.overstep == "none":
                 off = f"({oz}) * (int64_t)sz + ({oy}) * (int64_t)sy + ({ox})"
@@ -997,10 +999,153 @@ class SweepGroupEmitter:
         env = SweepEnv(self.gen, self.hoist_map, names, self.div_map, self.mul_map)
         return lines, self.gen.expr(sweep.stmt.value, env)
 
+    @staticmethod
+    def _row_base(oz: int, oy: int) -> str:
+        def part(a, o):
+            return f"{a}{'m' if o < 0 else 'p'}{abs(o)}" if o else f"{a}0"
+        return f"rb_{part('z', oz)}_{part('y', oy)}"
+
+    def zmarch_ok(self, mains: list, bnd_phases: list) -> bool:
+        """3-D single-sweep launch whose loads at a z offset have no y/x offset
+        (7-point style) and whose edges wrap or clamp: mask-free tiles walk z."""
+        if bnd_phases or len(mains) != 1 or self.gen.cfg.overstep == "none":
+            return False
+        s = self.g.sweeps[mains[0]]
+        if any(s.store_offset):
+            return False
+        for slot in self.slots_used([s]):
+            t = self.gen.defn.signature.arguments[self.arg_index(slot)][1]
+            if t.dimension != 3:
+                return False
+        for _, ld in s.loads:
+            oz, oy, ox = ld.offset
+            if abs(oz) > 1 or (oz and (oy or ox)):
+                return False
+        return True
+
+    def zmarch_body(self, j: int, mask_var: str) -> list:
+        """Mask-free tiles: every thread owns one (y, x) column of the tile and walks
+        it through z.  Loads at z +- 1 come from a three-value register window per
+        buffer, loads at y/x offsets from memory at the current plane through
+        per-column offsets that are wrapped (or clamped) once per thread.  Same
+        arithmetic per cell as the other paths."""
+        s = self.g.sweeps[j]
+        dst = self.bname((s.slot, s.level, s.write_version))
+        hor = sorted({(ld.offset[1], ld.offset[2]) for _, ld in s.loads if ld.offset[0] == 0})
+        if (0, 0) not in hor:
+            hor.append((0, 0))
+        vert = {}  # buffer -> set of z offsets
+        for _, ld in s.loads:
+            if ld.offset[1] == 0 and ld.offset[2] == 0:
+                vert.setdefault(self.bname((ld.slot, ld.level, ld.version)), set()).add(ld.offset[0])
+        win = {b: zs for b, zs in vert.items() if zs & {-1, 1}}
+        ys = sorted({oy for oy, _ in hor if oy})
+        xs = sorted({ox for _, ox in hor if ox})
+
+        def off(oy, ox):
+            return f"o_{'m' if oy < 0 else 'p'}{abs(oy)}_{'m' if ox < 0 else 'p'}{abs(ox)}"
+        L = [f"  if ({mask_var} && p.same) {{",
+             "    for (int y = y0 + (int)threadIdx.y; y < y1; y += (int)blockDim.y)",
+             "    for (int x = x0 + (int)threadIdx.x; x < x1; x += (int)blockDim.x) {"]
+        L += [f"      const int {self.axis_name('y', o)} = xg_axis(xg_overstep, y + ({o}), (int)p.Y);" for o in ys]
+        L += [f"      const int {self.axis_name('x', o)} = xg_axis(xg_overstep, x + ({o}), (int)p.X);" for o in xs]
+        L += [f"      const I {off(oy, ox)} = (I){self.axis_name('y', oy)} * sy + (I){self.axis_name('x', ox)};"
+              for oy, ox in hor]
+        c0 = off(0, 0)
+        if any(-1 in zs for zs in win.values()):
+            L.append("      const int zlo = xg_axis(xg_overstep, z0 - 1, (int)p.Z);")
+        for b, zs in win.items():
+            t = self.elem(int(b[1:].split("_")[0]))
+            L.append(f"      {t} w{b}_m = {b}[(I){'zlo' if -1 in zs else 'z0'} * sz + {c0}];")
+            L.append(f"      {t} w{b}_c = {b}[(I)z0 * sz + {c0}];")
+        def plane(ind, zb, names_of, tag):
+            """Loads and store of one plane: zb its base, names_of(buffer, oz) the window values."""
+            out, names, local = [], {}, {}
+            for st, ld in s.loads:
+                b = self.bname((ld.slot, ld.level, ld.version))
+                oz, oy, ox = ld.offset
+                if b in win and oy == 0 and ox == 0:
+                    names[id(st)] = names_of(b, oz)
+                    continue
+                if ld not in local:
+                    vn = f"h{tag}_{len(local)}"
+                    local[ld] = vn
+                    out.append(f"{ind}const {self.elem(ld.slot)} {vn} = {b}[{zb} + {off(oy, ox)}];")
+                names[id(st)] = local[ld]
+            env = SweepEnv(self.gen, self.hoist_map, names, self.div_map, self.mul_map)
+            return out, f"{ind}{dst}[{zb} + {c0}] = {self.gen.expr(s.stmt.value, env)};"
+
+        U = 4  # planes per step: the loads of U planes are in flight together
+        L += ["      int z = z0;",
+              f"      for (; z + {U} <= z1; z += {U}) {{",
+              "        const I zb0 = (I)z * sz;"]
+        L += [f"        const I zb{k} = zb{k - 1} + sz;" for k in range(1, U)]
+        if any(1 in zs for zs in win.values()):
+            L.append(f"        const int zn = xg_axis(xg_overstep, z + {U}, (int)p.Z);")
+        for b, zs in win.items():
+            t = self.elem(int(b[1:].split("_")[0]))
+            for k in range(U - 1):
+                L.append(f"        const {t} w{b}_{k + 1} = {b}[zb{k + 1} + {c0}];")
+            L.append(f"        const {t} w{b}_{U} = {b}[(I){'zn' if 1 in zs else f'(z + {U - 1})'} * sz + {c0}];")
+
+        def wname(k):
+            def names_of(b, oz):
+                idx = k + oz  # plane index relative to z: -1 -> w_m, 0 -> w_c, j >= 1 -> w_j
+                return f"w{b}_m" if idx == -1 else (f"w{b}_c" if idx == 0 else f"w{b}_{idx}")
+            return names_of
+        stores = []
+        for k in range(U):
+            loads, store = plane("        ", f"zb{k}", wname(k), str(k))
+            L += loads
+            stores.append(store)
+        L += stores
+        for b in win:
+            L += [f"        w{b}_m = w{b}_{U - 1};", f"        w{b}_c = w{b}_{U};"]
+        L += ["      }",
+              "      for (; z < z1; ++z) {",
+              "        const I zb = (I)z * sz;"]
+        if any(1 in zs for zs in win.values()):
+            L.append("        const int zn = xg_axis(xg_overstep, z + 1, (int)p.Z);")
+        for b, zs in win.items():
+            t = self.elem(int(b[1:].split("_")[0]))
+            L.append(f"        const {t} w{b}_p = {b}[(I){'zn' if 1 in zs else 'z'} * sz + {c0}];")
+        loads, store = plane("        ", "zb", lambda b, oz: f"w{b}_{'m' if oz < 0 else ('p' if oz > 0 else 'c')}", "r")
+        L += loads + [store]
+        for b in win:
+            L += [f"        w{b}_m = w{b}_c;", f"        w{b}_c = w{b}_p;"]
+        L.append("      }")
+        L += ["    }", "  }"]
+        return L
+
+    def edge_row_loop(self, mains: list, indent: str) -> list:
+        """Cell loop of edge tiles under wrap/limit: the wrapped (or clamped) z and
+        y coordinates and the row base of every (z, y) offset pair are computed
+        once per row, only the x coordinates once per cell."""
+        sweeps = [self.g.sweeps[j] for j in mains]
+        pairs = sorted({(ld.offset[0], ld.offset[1]) for s in sweeps for _, ld in s.loads})
+        zs = sorted({oz for oz, _ in pairs if oz})
+        ys = sorted({oy for _, oy in pairs if oy})
+        out = [f"{indent}for (int z = z0; z < z1; ++z)",
+               f"{indent}for (int y = y0 + (int)threadIdx.y; y < y1; y += (int)blockDim.y) {{",
+               f"{indent}  const I row_ = (I)z * sz + (I)y * sy;"]
+        out += [f"{indent}  const int {self.axis_name('z', o)} = xg_axis(xg_overstep, z + ({o}), (int)p.Z);"
+                for o in zs]
+        out += [f"{indent}  const int {self.axis_name('y', o)} = xg_axis(xg_overstep, y + ({o}), (int)p.Y);"
+                for o in ys]
+        out += [f"{indent}  const I {self._row_base(oz, oy)} = (I){self.axis_name('z', oz)} * sz + "
+                f"(I){self.axis_name('y', oy)} * sy;" for oz, oy in pairs]
+        out += [f"{indent}  for (int x = x0 + (int)threadIdx.x; x < x1; x += (int)blockDim.x) {{",
+                f"{indent}  const I c = row_ + (I)x;"]
+        return out
+
     def main_body(self, sweeps_idx: list, fast, indent: str, mask_vars: dict) -> list:
         lines = []
         if fast == "edge":
             lines += self.axis_decls([self.g.sweeps[j] for j in sweeps_idx], indent)
+        elif fast == "edge_row":
+            xs = sorted({ld.offset[2] for j in sweeps_idx for _, ld in self.g.sweeps[j].loads if ld.offset[2]})
+            lines += [f"{indent}const int {self.axis_name('x', o)} = xg_axis(xg_overstep, x + ({o}), (int)p.X);"
+                      for o in xs]
         for j in sweeps_idx:
             s = self.g.sweeps[j]
             dst = self.bname((s.slot, s.level, s.write_version))
@@ -1114,7 +1259,9 @@ class SweepGroupEmitter:
                 for a in range(3):
                     lo[a] = min(lo[a], ld.offset[a])
                     hi[a] = max(hi[a], ld.offset[a])
-        lines = [f"template <typename I> __global__ void __launch_bounds__(256, {self.min_blocks()}) xgk_{n}_{gid}_{tag}("
+        zm = self.zmarch_ok(mains, bnd_phases)
+        blocks = 3 if zm else self.min_blocks()  # the z walk keeps several planes' loads in registers
+        lines = [f"template <typename I> __global__ void __launch_bounds__(256, {blocks}) xgk_{n}_{gid}_{tag}("
                  f"const __grid_constant__ struct xgp_{n}_{gid}_{tag} p) {{"] + TILE_PROLOGUE + \
             self.restrict_locals([self.g.sweeps[j] for j in list(mains) + list(bnd_phases)]) + [
                  f"  const bool fast = p.same && z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && "
@@ -1124,7 +1271,11 @@ class SweepGroupEmitter:
             mask_vars[j] = f"mz{j}"
             lines.append(f"  const bool mz{j} = p.tzero{j}[t] != 0;")
         R = self.rows_for(mains)
-        lines.append("  if (fast) {")
+        if zm:
+            lines += self.zmarch_body(mains[0], mask_vars[mains[0]])
+            lines.append("  else if (fast) {")
+        else:
+            lines.append("  if (fast) {")
         if R:
             lines += self.rows_loop(mains[0], mask_vars[mains[0]], "    ", "fast", R)
         else:
@@ -1134,6 +1285,10 @@ class SweepGroupEmitter:
         lines.append("  } else if (p.same) {")
         if R:
             lines += self.rows_loop(mains[0], mask_vars[mains[0]], "    ", "edge", R)
+        elif self.gen.cfg.overstep != "none":
+            lines += self.edge_row_loop(mains, "    ")
+            lines += self.main_body(mains, "edge_row", "      ", mask_vars)
+            lines.append("    }}")
         else:
             lines += ["  " + l for l in CELL_LOOP]
             lines += self.main_body(mains, "edge", "      ", mask_vars)
