@@ -153,8 +153,8 @@ class BatchEmitter:
               "      for (int lx = threadIdx.x; lx < RX; lx += blockDim.x) {",
               "        int gx = x0 - HX + lx;",
               "        gx = gx < 0 ? gx + X : (gx >= X ? gx - X : gx);"]
-        K += [f"        sA{f}[ly * PX + lx] = in{f}[row + gx];" for f in fields]
-        K += ["      }", "    }", "    __syncthreads();"]
+        K += [f"        xg_cp_async(&sA{f}[ly * PX + lx], &in{f}[row + gx]);" for f in fields]
+        K += ["      }", "    }", "    xg_cp_async_wait_all();", "    __syncthreads();"]
 
         def body(indent, store):
             out = []

@@ -520,3 +520,15 @@ __device__ __forceinline__ double xg_dadd_core(double a, double b) {
 
 __device__ __forceinline__ double xg_dadd_i(double a, double b) { return xg_dadd_core<false>(a, b); }
 __device__ __forceinline__ double xg_dsub_i(double a, double b) { return xg_dadd_core<true>(a, b); }
+
+// Asynchronous copy of one element from global to shared memory (cp.async): a
+// thread issues all of its tile's copies back to back without a register round
+// trip, then waits once (xg_cp_async_wait_all) before the block barrier.
+template <typename T>
+__device__ __forceinline__ void xg_cp_async(T* dst, const T* src) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "cp.async copies 4, 8 or 16 bytes");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(xg_smem_addr(dst)), "l"(src), "n"(sizeof(T))
+               : "memory");
+}
+
+__device__ __forceinline__ void xg_cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
