@@ -35,6 +35,11 @@ from .types import Floating, GridType
 B = ir.BinaryOperator
 LOG = Logger("xgrid.adjoint")
 
+# z-walk of the adjoint kernel: planes whose loads are issued together, and resident
+# 256-thread CTAs per SM asked of ptxas (registers: planes x buffers x loads per plane)
+ZWALK_PLANES = 2
+ZWALK_BLOCKS = 3
+
 
 # ------------------------------------------------------------ symbolic algebra
 # nodes: ("c", float) | ("p", name) | ("l", (slot, level, offset)) | (op, a, b) | ("neg", a)
@@ -295,13 +300,111 @@ class AdjointGenerator:
                     out.append(f"      if (p.g{slot}) p.g{slot}[c] = p.g{slot}[c] + ({total});")
             return out
 
-        K = [f"template <typename I> __global__ void __launch_bounds__(256, 4) xgk_{n}_adjoint("
-             f"const __grid_constant__ struct xgadj_{n} p) {{"] + TILE_PROLOGUE + [
-             f"  const bool fast = z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && y0 + ({lo[1]}) >= 0 && "
-             f"y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;",
-             "  if (fast) {"]
-        K += ["  " + l for l in CELL_LOOP] + body(True) + ["    }}", "  } else {"]
-        K += ["  " + l for l in CELL_LOOP] + body(False) + ["    }}", "  }", "}"]
+        def outputs(idx: str, ind: str) -> list:
+            out = []
+            for slot in slots_used:
+                acc = []
+                for off, d in terms.get(slot, []):
+                    lam = names[("lam", tuple(-o for o in off))]
+                    acc.append(f"({lam} * {self.emit_sym(d, loadname)})")
+                total = " + ".join(acc) if acc else f"(({T})0)"
+                if slot == self.slot:
+                    out.append(f"{ind}p.lam_out[{idx}] = {total};")
+                else:
+                    out.append(f"{ind}if (p.g{slot}) p.g{slot}[{idx}] = p.g{slot}[{idx}] + ({total});")
+            return out
+
+        # z-walk (7-point loads, wrapped or clamped edges): every thread walks one (y, x) column
+        # through z, z-neighbours from a register window per buffer, four planes per step
+        bufs = {}
+        for off in lam_offsets:
+            bufs.setdefault("lam", ("p.lam_in", set()))[1].add(off)
+        for slot, level, off in loads_needed:
+            bufs.setdefault((slot, level), (f"p.f{slot}[{level}]", set()))[1].add(off)
+        zwalk = not none_mode and all(abs(o[0]) <= 1 and (o[0] == 0 or (o[1] == 0 and o[2] == 0))
+                                      for _, offs in bufs.values() for o in offs)
+
+        def zwalk_body() -> list:
+            hor = sorted({(o[1], o[2]) for _, offs in bufs.values() for o in offs if o[0] == 0} | {(0, 0)})
+            win = {k: offs for k, (_, offs) in bufs.items() if any(o[0] for o in offs)}
+            ys = sorted({oy for oy, _ in hor if oy})
+            xs = sorted({ox for _, ox in hor if ox})
+
+            def off(oy, ox):
+                return f"o_{'m' if oy < 0 else 'p'}{abs(oy)}_{'m' if ox < 0 else 'p'}{abs(ox)}"
+
+            def wv(k):
+                return "lam" if k == "lam" else f"f{k[0]}_{k[1]}"
+            c0 = off(0, 0)
+            L = ["  for (int y = y0 + (int)threadIdx.y; y < y1; y += (int)blockDim.y)",
+                 "  for (int x = x0 + (int)threadIdx.x; x < x1; x += (int)blockDim.x) {"]
+            L += [f"    const int {axis_name('y', o)} = xg_axis(xg_overstep, y + ({o}), (int)p.Y);" for o in ys]
+            L += [f"    const int {axis_name('x', o)} = xg_axis(xg_overstep, x + ({o}), (int)p.X);" for o in xs]
+            L += [f"    const I {off(oy, ox)} = (I){axis_name('y', oy)} * sy + (I){axis_name('x', ox)};"
+                  for oy, ox in hor]
+            L.append("    const int zlo = xg_axis(xg_overstep, z0 - 1, (int)p.Z);")
+            for k in win:
+                ptr = bufs[k][0]
+                L += [f"    {T} w{wv(k)}_m = {ptr}[(I)zlo * sz + {c0}];",
+                      f"    {T} w{wv(k)}_c = {ptr}[(I)z0 * sz + {c0}];"]
+
+            def plane(ind, zb, idx_of, tag):
+                out = []
+                for k, (ptr, offs) in bufs.items():
+                    for o in sorted(offs):
+                        key = ("lam", o) if k == "lam" else (k[0], k[1], o)
+                        if k in win and o[1] == 0 and o[2] == 0:
+                            names[key] = idx_of(k, o[0])
+                            continue
+                        vn = f"h{tag}_{wv(k)}_{off(o[1], o[2])}"
+                        out.append(f"{ind}const {T} {vn} = {ptr}[{zb} + {off(o[1], o[2])}];")
+                        names[key] = vn
+                return out
+
+            U = ZWALK_PLANES
+            L += ["    int z = z0;",
+                  f"    for (; z + {U} <= z1; z += {U}) {{",
+                  "      const I zb0 = (I)z * sz;"]
+            L += [f"      const I zb{i} = zb{i - 1} + sz;" for i in range(1, U)]
+            L.append(f"      const int zn = xg_axis(xg_overstep, z + {U}, (int)p.Z);")
+            for k in win:
+                ptr = bufs[k][0]
+                L += [f"      const {T} w{wv(k)}_{i + 1} = {ptr}[zb{i + 1} + {c0}];" for i in range(U - 1)]
+                L.append(f"      const {T} w{wv(k)}_{U} = {ptr}[(I)zn * sz + {c0}];")
+            outs = []
+            for i in range(U):
+                def idx_of(k, oz, i=i):
+                    j = i + oz
+                    return f"w{wv(k)}_m" if j == -1 else (f"w{wv(k)}_c" if j == 0 else f"w{wv(k)}_{j}")
+                L += plane("      ", f"zb{i}", idx_of, str(i))
+                outs += outputs(f"zb{i} + {c0}", "      ")
+            L += outs
+            for k in win:
+                prev = f"w{wv(k)}_c" if U == 1 else f"w{wv(k)}_{U - 1}"
+                L += [f"      w{wv(k)}_m = {prev};", f"      w{wv(k)}_c = w{wv(k)}_{U};"]
+            L += ["    }",
+                  "    for (; z < z1; ++z) {",
+                  "      const I zb = (I)z * sz;",
+                  "      const int zn = xg_axis(xg_overstep, z + 1, (int)p.Z);"]
+            for k in win:
+                L.append(f"      const {T} w{wv(k)}_p = {bufs[k][0]}[(I)zn * sz + {c0}];")
+            L += plane("      ", "zb", lambda k, oz: f"w{wv(k)}_{'m' if oz < 0 else ('p' if oz > 0 else 'c')}", "r")
+            L += outputs(f"zb + {c0}", "      ")
+            for k in win:
+                L += [f"      w{wv(k)}_m = w{wv(k)}_c;", f"      w{wv(k)}_c = w{wv(k)}_p;"]
+            L += ["    }", "  }"]
+            return L
+
+        K = [f"template <typename I> __global__ void __launch_bounds__(256, {ZWALK_BLOCKS if zwalk else 4}) xgk_{n}_adjoint("
+             f"const __grid_constant__ struct xgadj_{n} p) {{"] + TILE_PROLOGUE
+        if zwalk:
+            K += zwalk_body() + ["}"]
+        else:
+            K += [f"  const bool fast = z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && y0 + ({lo[1]}) >= 0 && "
+                  f"y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;",
+                  "  if (fast) {"]
+            K += ["  " + l for l in CELL_LOOP] + body(True) + ["    }}", "  } else {"]
+            K += ["  " + l for l in CELL_LOOP] + body(False) + ["    }}", "  }", "}"]
         ns = len(gen.slots)
         value_args = [(a, t) for a, t in gen.defn.signature.arguments if not isinstance(t, GridType)]
         H = [f'extern "C" int xg_adjoint_{n}(void* lam_out, const void* lam_in, const void* const* fields, '
@@ -324,7 +427,7 @@ class AdjointGenerator:
             for lv in range(gen.depth + 1):
                 H.append(f"  p.f{slot}[{lv}] = (const {T}*)fields[{slot} * {gen.depth + 1} + {lv}];")
             H.append(f"  p.g{slot} = ({T}*)grads[{slot}];")
-        H += ["  p.tz = 2; p.ty = 16; p.tx = 32;",
+        H += [f"  p.tz = {32 if zwalk else 2}; p.ty = {8 if zwalk else 16}; p.tx = 32;",
               "  p.ntz = xg_tiles_along(p.Z, p.tz); p.nty = xg_tiles_along(p.Y, p.ty); p.ntx = xg_tiles_along(p.X, p.tx);",
               "  dim3 grid, block(32, 8, 1);",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
