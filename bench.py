@@ -43,6 +43,10 @@ SWEEPS_PER_STEP = 54  # b, 1 + 50 Jacobi, u, v
 DT = {1025: 5e-6, 4097: 5e-7}
 
 
+def workload_name(n: int) -> str:
+    return f"lid-driven cavity {n}x{n} FP64 plain, dt={stable_dt(n):g}, 50+1 Jacobi sweeps/step"
+
+
 def stable_dt(n: int) -> float:
     if n in DT:
         return DT[n]
@@ -253,6 +257,40 @@ def replica_time(secs: float, world: int, device: str = "cuda") -> float:
     return float(t.item())
 
 
+def fp64_peak(n: int = 2048, calls: int = 10) -> float:
+    """FP64 additions per second of the FP64 unit, measured with the DSL probe
+    (32 chained additions per cell, fields resident in L2)."""
+    import numpy as np
+    import torch
+
+    import xgrid
+    import workloads
+    from xgrid_gb300 import device
+    from xgrid_gb300.operator import Operator
+    xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+               opt_level=3)
+    k = Operator(workloads.fp64_probe.func, "kernel", "fp64_probe")
+    q, x = xgrid.Grid((n, n), float), xgrid.Grid((n, n), float)
+    x.now[...] = np.random.default_rng(0).random((n, n))
+    for _ in range(3):
+        k(q, x, 1e-3)
+    s = device.stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.synchronize()
+    e0.record(s)
+    for _ in range(calls):
+        k(q, x, 1e-3)
+    e1.record(s)
+    s.synchronize()
+    return workloads.FP64_PROBE_ADDS * n * n * calls / (e0.elapsed_time(e1) * 1e-3)
+
+
+# FP64 operations per cell of the cavity's Jacobi sweep after host hoisting: 3 additions and 1
+# subtraction; the products by dx^2, dy^2 and the quotient by 2(dx^2+dy^2) are exact exponent
+# arithmetic on the integer pipe when dx = dy = 2/(n-1) is a power of two (n = 2^k + 1).
+JACOBI_FP64_OPS = 4
+
+
 def gpu_bench(args, rank: int, world: int):
     import torch
 
@@ -327,6 +365,15 @@ def gpu_bench(args, rank: int, world: int):
     hbm_peak, peak_src = peaks()
     achieved = alg_bytes / dom_avg_s / 1e9
     traffic, traffic_src = profile_traffic("cavity_jacobi_fused_fp64", n)
+    pow2 = ((n - 1) & (n - 2)) == 0
+    fp64 = None
+    if pow2:
+        peak64 = fp64_peak()
+        rate64 = JACOBI_FP64_OPS * n * n / dom_avg_s
+        fp64 = {"bound": "fp64 pipe", "achieved_gops": rate64 / 1e9, "peak_gops": peak64 / 1e9,
+                "frac": rate64 / peak64, "ops_per_cell": JACOBI_FP64_OPS,
+                "peak_source": "32-addition FP64 probe sweep measured in this run (L2-resident 2048^2)"}
+        xgrid.init(precision="double", cacheroot=cache, opt_level=3)
 
     # e2e through the public API with host buffers
     for g in (u, v, p):
@@ -358,15 +405,15 @@ def gpu_bench(args, rank: int, world: int):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic: zero initial fields, lid u=1 (deterministic)",
-        "config": {"workload": f"lid-driven cavity {n}x{n} FP64 plain, dt={stable_dt(n):g}, 50+1 Jacobi "
-                               f"sweeps/step, bit-exact vs reference C",
+        "config": {"workload": workload_name(n), "parity": "bit-exact vs the reference's C",
                    "n": n, "sweeps_per_step": SWEEPS_PER_STEP, "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}", "graph": True, "launches_per_step": launches_per_step},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "traffic_source": traffic_src,
                      "peak_source": peak_src,
                      "kernel": f"group {group} (site {dom_site})", "kernel_ms": dom_avg_s * 1e3,
-                     "kernel_share": sum(dom_ms) / total_prof, "algorithmic_bytes_per_launch": alg_bytes},
+                     "kernel_share": sum(dom_ms) / total_prof, "algorithmic_bytes_per_launch": alg_bytes,
+                     "fp64": fp64},
         "e2e": e2e,
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clk.summary(),
@@ -607,9 +654,7 @@ def reference_arm(args, rank: int, world: int):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["seconds"] / r["steps"] * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: zero initial fields, lid u=1 (deterministic)",
-        "config": {"workload": f"lid-driven cavity {n}x{n} FP64 plain, dt={stable_dt(n):g}, 50+1 Jacobi "
-                               f"sweeps/step", "n": n,
-                   "sweeps_per_step": SWEEPS_PER_STEP},
+        "config": {"workload": workload_name(n), "n": n, "sweeps_per_step": SWEEPS_PER_STEP},
         "cpu_baseline": {"value": val, "unit": "GLUP/s", "cores": r["cores"], "kind": r["kind"],
                          "sample": f"cavity {n}x{n} FP64, {r['steps']} steps ({r['seconds']:.1f} s)"},
         "e2e": {"value": val, "unit": "GLUP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

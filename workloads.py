@@ -133,6 +133,17 @@ def cavity_setup(n: int = 1025, dt: float = 1e-5):
     return grids, cfg
 
 
+# ---------------------------------------------------------- FP64 rate probe
+@xgrid.kernel()
+def fp64_probe(q: float2d, x: float2d, a: float) -> None:
+    # 32 dependent FP64 additions per cell (no subtree is free of the load, so none
+    # is hoisted): on an L2-resident grid the sweep measures the FP64 add rate
+    q[0, 0] = x[0, 0] + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a + a
+
+
+FP64_PROBE_ADDS = 32
+
+
 # ----------------------------------------------------------- batched problems
 @xgrid.kernel()
 def convdiff2d(u: float2d, a0: float, axm: float, axp: float, aym: float, ayp: float) -> None:
