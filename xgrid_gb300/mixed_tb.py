@@ -30,9 +30,7 @@ from __future__ import annotations
 
 from . import analysis
 
-BX = 128          # box columns = threads along x
-STRIPS = 2        # thread rows; the box has STRIPS * RS rows
-ROWS = (8, 16, 24)
+BX = 128          # box columns = threads along x; the block has two rows of threads (strips)
 DSCALE = 8        # defect: an input of largest magnitude m is stored as m * 2^s in [2^8, 2^9)
 RSCALE = 14       # residual (fixed over the loop): [2^14, 2^15), below the FP16 maximum
 STORAGE = {"fp32": ("float", 0, "CU_TENSOR_MAP_DATA_TYPE_FLOAT32"),
@@ -121,7 +119,7 @@ class TemporalDefect:
         K = [f"template <typename Dt, int RS>",
              f"__global__ void __launch_bounds__(256, RS <= 8 ? 4 : (RS <= 16 ? 3 : 2)) xgk_{n}_{gid}_mxt(const __grid_constant__ "
              f"struct xgp_{n}_{gid}_mxt p) {{",
-             "  constexpr int BX = 128, BY = 2 * RS;",
+             f"  constexpr int BX = {BX}, BY = 2 * RS;",
              "  constexpr bool scaled = sizeof(Dt) == 2;",
              "  extern __shared__ unsigned char xg_dsm[];",
              "  __shared__ __align__(8) uint64_t xg_bar;",
@@ -266,7 +264,7 @@ class TemporalDefect:
              f"  *RS = xg_mxt_{n}[1];",
              "  if (*RS != 8 && *RS != 16 && *RS != 24) return 0;",
              f"  halo[0] = 0; halo[1] = *T * {self.sy}; halo[2] = (*T * {self.sx} + 7) / 8 * 8;",
-             "  core[0] = 1; core[1] = 2 * *RS - 2 * halo[1]; core[2] = 128 - 2 * halo[2];",
+             f"  core[0] = 1; core[1] = 2 * *RS - 2 * halo[1]; core[2] = {BX} - 2 * halo[2];",
              "  if (core[1] < 1 || core[2] < 8) return 0;",
              f"  const int32_t shrink[3] = {{0, {self.sy}, {self.sx}}};"]
         L += arr("mo", mo) + arr("vals", vals) + arr("nof", nof) + arr("offs", offs)
@@ -279,10 +277,10 @@ class TemporalDefect:
               f"static int xgm_{n}_{gid}_go(const struct xgp_{n}_{gid}_mxt& p, int64_t nt, cudaStream_t s) {{",
               "  static int avail = -1;",
               f"  if (avail < 0) XG_TRY(xg_smem_optin(xgk_{n}_{gid}_mxt<{dt}, RS>, &avail));",
-              "  const size_t smem = (size_t)2 * (2 * RS) * 128 * sizeof(float) + 1024;",
+              f"  const size_t smem = (size_t)2 * (2 * RS) * {BX} * sizeof(float) + 1024;",
               "  if (smem > (size_t)avail) XG_FAIL(\"temporal blocking: %zu bytes of shared memory, %d available\", "
               "smem, avail);",
-              f"  xgk_{n}_{gid}_mxt<{dt}, RS><<<(unsigned)nt, dim3(128, 2, 1), smem, s>>>(p);",
+              f"  xgk_{n}_{gid}_mxt<{dt}, RS><<<(unsigned)nt, dim3({BX}, 2, 1), smem, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
               "  return 0;",
               "}",
@@ -299,11 +297,11 @@ class TemporalDefect:
               "  p.dep = dep; p.first = first; p.li = li;",
               "  const int BY = 2 * RS;",
               f"  const int es = (int)sizeof({dt});",
-              f"  if (!first) XG_TRY(xg_tmap_2d(&p.md, din, {self.cutype}, es, e.x, e.y, A->XP * es, 128, BY));",
+              f"  if (!first) XG_TRY(xg_tmap_2d(&p.md, din, {self.cutype}, es, e.x, e.y, A->XP * es, {BX}, BY));",
               f"  if (first || !{int(self.scaled)})",
-              "    XG_TRY(xg_tmap_2d(&p.mr, A->r32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, e.x, e.y, A->XP * 4, 128, BY));",
+              f"    XG_TRY(xg_tmap_2d(&p.mr, A->r32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, e.x, e.y, A->XP * 4, {BX}, BY));",
               "  else",
-              f"    XG_TRY(xg_tmap_2d(&p.mr, A->r16, {self.cutype}, es, e.x, e.y, A->XP * es, 128, BY));",
+              f"    XG_TRY(xg_tmap_2d(&p.mr, A->r16, {self.cutype}, es, e.x, e.y, A->XP * es, {BX}, BY));",
               "  p.dout = dout;",
               f"  p.rout = (first && {int(self.scaled)}) ? A->r16 : NULL;",
               "  p.sl = A->slots;",
