@@ -36,6 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SWEEPS_PER_STEP = 54  # b, 1 + 50 Jacobi, u, v
+JIT_CACHE = os.path.join(ROOT, ".xgrid_cache", "bench")  # compiled kernel modules stay in the tree
 # The configured dt = 1e-5 breaks the explicit-diffusion stability limit
 # nu*dt*(1/dx^2 + 1/dy^2) <= 1/2 (0.52 at 1025^2, 8.4 at 4097^2) and the fields
 # diverge after a few hundred steps; the benchmark uses the largest round dt
@@ -92,7 +93,7 @@ def kernels_only(args) -> None:
     import workloads
     from xgrid_gb300 import device
     if args.workload == "batch":
-        xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+        xgrid.init(precision="float", cacheroot=JIT_CACHE,
                    opt_level=3, overstep="wrap")
         probs = workloads.batch_setup(256, seed=1)
         temporal = None
@@ -109,7 +110,7 @@ def kernels_only(args) -> None:
         import torch
         from xgrid_gb300 import adjoint
         from xgrid_gb300.operator import Operator
-        xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+        xgrid.init(precision="float", cacheroot=JIT_CACHE,
                    opt_level=3, overstep="wrap")
         k = Operator(workloads.diffuse3d.func, "kernel", "diffuse3d")
         u0, kap, tgt, dt = workloads.adjoint_setup(args.n, 2)
@@ -121,7 +122,7 @@ def kernels_only(args) -> None:
         device.synchronize()
         print(json.dumps({"mode": "kernels", "workload": "adjoint", "n": args.n, "calls": args.warmup + 1}))
         return
-    xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+    xgrid.init(precision="double", cacheroot=JIT_CACHE,
                opt_level=3, mixed=args.mixed, mixed_temporal=args.mixed_temporal)
     grids, cfg = workloads.cavity_setup(args.n, stable_dt(args.n))
     for _ in range(args.warmup + args.steps):
@@ -267,7 +268,7 @@ def fp64_peak(n: int = 2048, calls: int = 10) -> float:
     import workloads
     from xgrid_gb300 import device
     from xgrid_gb300.operator import Operator
-    xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+    xgrid.init(precision="double", cacheroot=JIT_CACHE,
                opt_level=3)
     k = Operator(workloads.fp64_probe.func, "kernel", "fp64_probe")
     q, x = xgrid.Grid((n, n), float), xgrid.Grid((n, n), float)
@@ -299,7 +300,7 @@ def gpu_bench(args, rank: int, world: int):
     from xgrid_gb300 import device, runtime
 
     torch.cuda.set_device(rank % max(torch.cuda.device_count(), 1))
-    cache = os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}")
+    cache = JIT_CACHE
     xgrid.init(precision="double", cacheroot=cache, opt_level=3)
     n = args.n
     grids, cfg = workloads.cavity_setup(n, stable_dt(n))
@@ -439,7 +440,7 @@ def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
     dt = stable_dt(n)
     out, fields = {}, {}
     for mode in (None, "fp32", "fp16", "bf16"):
-        xgrid.init(precision="double", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+        xgrid.init(precision="double", cacheroot=JIT_CACHE,
                    opt_level=3, mixed=mode, mixed_temporal=temporal)
         k = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
         grids, cfg = workloads.cavity_setup(n, dt)
@@ -486,7 +487,7 @@ def batch_section(count: int, steps: int, seq_steps: int) -> dict:
     from xgrid_gb300 import device
     from xgrid_gb300.operator import Operator
 
-    xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+    xgrid.init(precision="float", cacheroot=JIT_CACHE,
                opt_level=3, overstep="wrap")
     k = Operator(workloads.convdiff2d.func, "kernel", "convdiff2d")
     probs = workloads.batch_setup(count, seed=1)
@@ -551,7 +552,7 @@ def adjoint_section(n: int, steps: int, every: int, torch_n: int) -> dict:
     from xgrid_gb300 import adjoint, device
     from xgrid_gb300.operator import Operator
 
-    xgrid.init(precision="float", cacheroot=os.path.join(tempfile.gettempdir(), f"xgbench_{os.getuid()}"),
+    xgrid.init(precision="float", cacheroot=JIT_CACHE,
                opt_level=3, overstep="wrap")
     k = Operator(workloads.diffuse3d.func, "kernel", "diffuse3d")
 

@@ -14,5 +14,9 @@ def pytest_configure(config):
 
 
 @pytest.fixture(scope="session")
-def cacheroot(tmp_path_factory):
-    return str(tmp_path_factory.mktemp("xgcache"))
+def cacheroot():
+    """Cache root of the kernel modules the tests compile: inside the tree, so the
+    loaded modules are the repository's own (md5-named, safe to share between runs)."""
+    path = os.path.join(ROOT, ".xgrid_cache", "tests")
+    os.makedirs(path, exist_ok=True)
+    return path

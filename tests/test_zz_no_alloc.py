@@ -9,6 +9,7 @@ the module instead of from the caller.  This file runs last so that a failure
 here does not hide the other tests' results.
 """
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -65,8 +66,14 @@ def _call_noalloc(p, f, iters: int, h2: float) -> int:
     return rc
 
 
+def _cache(tmp_path):
+    """A fresh module cache per test, inside the tree."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    return os.path.join(root, ".xgrid_cache", "noalloc", tmp_path.name)
+
+
 def test_noalloc_matches_regular_entry(tmp_path):
-    xgrid.init(precision="double", cacheroot=str(tmp_path), opt_level=3)
+    xgrid.init(precision="double", cacheroot=_cache(tmp_path), opt_level=3)
     n = 96
     pa, fa = _grids(n, 11)
     pb, fb = _grids(n, 11)
@@ -84,7 +91,7 @@ def test_noalloc_matches_regular_entry(tmp_path):
 
 
 def test_noalloc_refuses_to_build_tables(tmp_path):
-    xgrid.init(precision="double", cacheroot=str(tmp_path), opt_level=3)
+    xgrid.init(precision="double", cacheroot=_cache(tmp_path), opt_level=3)
     warm_p, warm_f = _grids(32, 1)
     relax(warm_p, warm_f, 1, 0.01)  # compiles the module
     p, f = _grids(40, 2)            # fresh masks: no tables yet
@@ -94,7 +101,7 @@ def test_noalloc_refuses_to_build_tables(tmp_path):
 
 
 def test_noalloc_rejects_grids_beyond_the_pool(tmp_path):
-    xgrid.init(precision="double", cacheroot=str(tmp_path), opt_level=3)
+    xgrid.init(precision="double", cacheroot=_cache(tmp_path), opt_level=3)
     warm_p, warm_f = _grids(32, 1)
     relax(warm_p, warm_f, 1, 0.01)
     p, f = _grids(3000, 3)          # 72 MB of FP64 scratch > 64 MiB
