@@ -66,6 +66,7 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default tile shapes of the headline kernel")
     ap.add_argument("--cpu-sample", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--mixed-n", type=int, default=4097)
     ap.add_argument("--mixed-steps", type=int, default=500)
@@ -310,6 +311,12 @@ def gpu_bench(args, rank: int, world: int):
     def step():
         kern(b, p, u, v, cfg)
 
+    tilings = None
+    if not args.no_tune:
+        # tile shape of every launch group picked by timing candidates on these grids
+        # (their state is restored afterwards; the choice is cached on disk per shape)
+        from xgrid_gb300 import autotune
+        tilings = {str(g): list(t) for g, t in autotune.tune(kern, b, p, u, v, cfg).items()}
     for _ in range(args.warmup):
         step()
     s = device.stream()
@@ -408,7 +415,8 @@ def gpu_bench(args, rank: int, world: int):
         "data": "synthetic: zero initial fields, lid u=1 (deterministic)",
         "config": {"workload": workload_name(n), "parity": "bit-exact vs the reference's C",
                    "n": n, "sweeps_per_step": SWEEPS_PER_STEP, "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": f"replicas x{world}", "graph": True, "launches_per_step": launches_per_step},
+                   "parallelism": f"replicas x{world}", "graph": True, "launches_per_step": launches_per_step,
+                   "tilings": tilings},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "traffic_source": traffic_src,
                      "peak_source": peak_src,
