@@ -97,3 +97,42 @@ def test_16bit_storage_within_tolerance_of_fp64(cacheroot, mode, tol):
     p = out["p"]
     assert (p[-1, :] == 0.0).all()
     assert (p[1:-1, -1] == p[1:-1, -2]).all() and (p[1:-1, 0] == p[1:-1, 1]).all()
+
+
+@xgrid.kernel()
+def relax_column(p: xgrid.grid[float, 2], f: xgrid.grid[float, 2], iters: int) -> None:
+    for _ in range(0, iters):
+        p[0, 0] = 0.25 * (p[1, 0][0] + p[-1, 0][0] + p[0, 1][0] + p[0, -1][0]) - 0.01 * f[0, 0][0]
+        with xgrid.boundary(1):
+            p[0, 0] = p[0, 1][0]
+        with xgrid.boundary(2):
+            p[0, 0] = 0.0
+
+
+@pytest.mark.parametrize("column,temporal_used", [(60, True), (118, False)])
+def test_box_check_accepts_and_rejects(cacheroot, column, temporal_used):
+    """A column of boundary cells that copies its right neighbour: deep inside a box
+    the temporal path runs; at column 118 (next to the inner edge of the first box,
+    128 columns with a halo of 8) the copy would read a stale cell, the check refuses
+    and the loop runs one iteration per launch.  Same bits either way."""
+    xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3, mixed="fp32")
+    k = Operator(relax_column.func, "kernel", "relax_column")
+    from xgrid_gb300.native import NativeKernel
+    k.native = NativeKernel(k)
+    lib = runtime.load()
+    out, launches = {}, {}
+    for T in (0, 4):
+        k.native.set_mixed_temporal(T, 16)
+        rng = np.random.default_rng(7)
+        p, f = xgrid.Grid((300, 300), float), xgrid.Grid((300, 300), float)
+        p.now[...] = rng.random((300, 300))
+        f.now[...] = rng.random((300, 300))
+        b = p.boundary
+        b[1:-1, column] = 1
+        b[0, :] = b[-1, :] = b[:, 0] = b[:, -1] = 2
+        lib.xg_prof_reset()
+        k(p, f, 30)
+        launches[T] = lib.xg_prof_launches()
+        out[T] = p.read(0)
+    assert out[0].tobytes() == out[4].tobytes()
+    assert (launches[4] < launches[0]) == temporal_used, launches
