@@ -175,8 +175,11 @@ def group_candidates(ndim: int) -> list:
         out = [(1, ty, tx, 32, 8, 1) for tx in (32, 64, 128) for ty in (8, 16, 32, 64)]
         out += [(1, ty, tx, 64, 4, 1) for tx in (64, 128) for ty in (16, 32, 64)]
         return out
-    return [(tz, ty, tx, 32, 8, 1) for tz, ty, tx in
-            ((1, 8, 32), (1, 16, 32), (1, 32, 32), (2, 8, 32), (2, 16, 32), (4, 8, 32), (1, 16, 64), (1, 8, 64))]
+    # 3-D: tall tiles for the z-walk of mask-free 7-point sweeps, flat ones for the generic loop
+    out = [(tz, ty, tx, 32, 8, 1) for tz, ty, tx in
+           ((1, 8, 32), (1, 16, 32), (2, 16, 32), (4, 8, 32), (32, 8, 32), (64, 8, 32))]
+    out += [(tz, 4, 64, 64, 4, 1) for tz in (16, 32, 64, 128)]
+    return out
 
 
 def tune(op, *args, calls: int = 2) -> dict:

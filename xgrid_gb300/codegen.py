@@ -43,8 +43,12 @@ from .types import (Boolean, Floating, GridType, Ignore, Integer, Pointer, Struc
 
 OVERSTEP = {"none": "XG_OVERSTEP_NONE", "limit": "XG_OVERSTEP_LIMIT", "wrap": "XG_OVERSTEP_WRAP"}
 
+# z-walk of 3-D sweeps: planes whose loads are issued together, resident 256-thread CTAs per SM
+ZWALK_PLANES = 4
+ZWALK_BLOCKS = 4
+
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
-DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 64, 32, 32, 8, 1), 3: (32, 8, 32, 32, 8, 1)}
+DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 64, 32, 32, 8, 1), 3: (64, 4, 64, 64, 4, 1)}
 
 # tile prologue and cell loop shared by the tile kernels (32-bit coordinates,
 # 64-bit linear index per row)
@@ -1075,7 +1079,7 @@ class SweepGroupEmitter:
             env = SweepEnv(self.gen, self.hoist_map, names, self.div_map, self.mul_map)
             return out, f"{ind}{dst}[{zb} + {c0}] = {self.gen.expr(s.stmt.value, env)};"
 
-        U = 4  # planes per step: the loads of U planes are in flight together
+        U = ZWALK_PLANES  # planes per step: the loads of U planes are in flight together
         L += ["      int z = z0;",
               f"      for (; z + {U} <= z1; z += {U}) {{",
               "        const I zb0 = (I)z * sz;"]
@@ -1100,7 +1104,7 @@ class SweepGroupEmitter:
             stores.append(store)
         L += stores
         for b in win:
-            L += [f"        w{b}_m = w{b}_{U - 1};", f"        w{b}_c = w{b}_{U};"]
+            L += [f"        w{b}_m = {f'w{b}_c' if U == 1 else f'w{b}_{U - 1}'};", f"        w{b}_c = w{b}_{U};"]
         L += ["      }",
               "      for (; z < z1; ++z) {",
               "        const I zb = (I)z * sz;"]
@@ -1260,7 +1264,7 @@ class SweepGroupEmitter:
                     lo[a] = min(lo[a], ld.offset[a])
                     hi[a] = max(hi[a], ld.offset[a])
         zm = self.zmarch_ok(mains, bnd_phases)
-        blocks = 3 if zm else self.min_blocks()  # the z walk keeps several planes' loads in registers
+        blocks = ZWALK_BLOCKS if zm else self.min_blocks()  # the z walk keeps several planes in registers
         lines = [f"template <typename I> __global__ void __launch_bounds__(256, {blocks}) xgk_{n}_{gid}_{tag}("
                  f"const __grid_constant__ struct xgp_{n}_{gid}_{tag} p) {{"] + TILE_PROLOGUE + \
             self.restrict_locals([self.g.sweeps[j] for j in list(mains) + list(bnd_phases)]) + [
