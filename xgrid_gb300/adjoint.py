@@ -38,7 +38,8 @@ LOG = Logger("xgrid.adjoint")
 # z-walk of the adjoint kernel: planes whose loads are issued together, and resident
 # 256-thread CTAs per SM asked of ptxas (registers: planes x buffers x loads per plane)
 ZWALK_PLANES = 2
-ZWALK_BLOCKS = 3
+ZWALK_BLOCKS = 4
+ZWALK_TILE = (64, 4, 64, 64, 4)  # tz, ty, tx, block x, block y
 
 
 # ------------------------------------------------------------ symbolic algebra
@@ -427,9 +428,10 @@ class AdjointGenerator:
             for lv in range(gen.depth + 1):
                 H.append(f"  p.f{slot}[{lv}] = (const {T}*)fields[{slot} * {gen.depth + 1} + {lv}];")
             H.append(f"  p.g{slot} = ({T}*)grads[{slot}];")
-        H += [f"  p.tz = {32 if zwalk else 2}; p.ty = {8 if zwalk else 16}; p.tx = 32;",
+        tz, ty, tx, bx, by = ZWALK_TILE if zwalk else (2, 16, 32, 32, 8)
+        H += [f"  p.tz = {tz}; p.ty = {ty}; p.tx = {tx};",
               "  p.ntz = xg_tiles_along(p.Z, p.tz); p.nty = xg_tiles_along(p.Y, p.ty); p.ntx = xg_tiles_along(p.X, p.tx);",
-              "  dim3 grid, block(32, 8, 1);",
+              f"  dim3 grid, block({bx}, {by}, 1);",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
               "  xg_prof_launch(-2, s);",
               f"  if (xg_small_index(p.Z, p.Y, p.X)) xgk_{n}_adjoint<int><<<grid, block, 0, s>>>(p);",
