@@ -969,6 +969,12 @@ class SweepGroupEmitter:
         False generic per-grid addressing."""
         b = self.bname((ld.slot, ld.level, ld.version))
         oz, oy, ox = ld.offset
+        if fast == "flat":
+            # overstep "none" with every grid of the launch in one shape: the reference's
+            # flattened neighbour ((z+oz)*Y + (y+oy))*X + (x+ox) is c plus a constant
+            e = f"p.e{sweep.slot}"
+            off = f"({oz}) * ({e}[1] * {e}[2]) + ({oy}) * {e}[2] + ({ox})"
+            return f"xg_ldc({b}, xg_flat((int64_t)c + {off}, {e}[0] * {e}[1] * {e}[2]))"
         if fast == "edge_row":
             return f"{b}[{self._row_base(oz, oy)} + (I){self.axis_name('x', ox)}]"
         if fast == "edge":
@@ -1311,12 +1317,17 @@ class SweepGroupEmitter:
                       "    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);",
                       "    const int nthr = blockDim.x * blockDim.y * blockDim.z;",
                       f"    for (int64_t e = p.bo{j}[t] + tid; e < p.bo{j}[t + 1]; e += nthr) {{",
-                      f"    const int64_t c = p.bc{j}[e];",
-                      f"    const int64_t x = c % p.e{s.slot}[2], y = (c / p.e{s.slot}[2]) % p.e{s.slot}[1], "
+                      f"    const int64_t c = p.bc{j}[e];"]
+            decode = [f"    const int64_t x = c % p.e{s.slot}[2], y = (c / p.e{s.slot}[2]) % p.e{s.slot}[1], "
                       f"z = c / (p.e{s.slot}[2] * p.e{s.slot}[1]);",
                       "    (void)x; (void)y; (void)z;"]
-            lines += pre
-            lines.append(f"    {dst}[c] = {val};")
+            if self.gen.cfg.overstep == "none":
+                # no coordinates needed when every grid has the launch's shape
+                fpre, fval = self.value_code(s, "flat", "      ")
+                lines += ["    if (p.same) {"] + fpre + [f"      {dst}[c] = {fval};", "    } else {"]
+                lines += ["  " + l for l in decode + pre] + [f"      {dst}[c] = {val};", "    }"]
+            else:
+                lines += decode + pre + [f"    {dst}[c] = {val};"]
             lines += ["    }", "  }"]
         if final:
             # a list of per-cell lines, or (lines before the cell loop, per-cell lines, lines after it)
