@@ -291,6 +291,8 @@ def fp64_peak(n: int = 2048, calls: int = 10) -> float:
 # subtraction; the products by dx^2, dy^2 and the quotient by 2(dx^2+dy^2) are exact exponent
 # arithmetic on the integer pipe when dx = dy = 2/(n-1) is a power of two (n = 2^k + 1).
 JACOBI_FP64_OPS = 4
+JACOBI_ITERS = 50     # pressure iterations of the loop in the cavity step
+LOOP_SITE = 61        # profiling site (group * 64 + 61) of a persistent loop launch
 
 
 def gpu_bench(args, rank: int, world: int):
@@ -368,16 +370,19 @@ def gpu_bench(args, rank: int, world: int):
     dom_avg_s = statistics.mean(dom_ms) / 1000.0
     total_prof = sum(sum(x) for x in by_site.values())
     group = dom_site // 64
+    # a persistent loop launch runs all 50 Jacobi iterations (+ boundary phases)
+    loop = dom_site % 64 == LOOP_SITE
+    iters = JACOBI_ITERS if loop else 1
     bytes_per_cell = algorithmic_bytes(native_k.module, group)
-    alg_bytes = bytes_per_cell * n * n
+    alg_bytes = bytes_per_cell * n * n * iters
     hbm_peak, peak_src = peaks()
     achieved = alg_bytes / dom_avg_s / 1e9
-    traffic, traffic_src = profile_traffic("cavity_jacobi_fused_fp64", n)
+    traffic, traffic_src = profile_traffic("cavity_jacobi_loop_fp64" if loop else "cavity_jacobi_fused_fp64", n)
     pow2 = ((n - 1) & (n - 2)) == 0
     fp64 = None
     if pow2:
         peak64 = fp64_peak()
-        rate64 = JACOBI_FP64_OPS * n * n / dom_avg_s
+        rate64 = JACOBI_FP64_OPS * n * n * iters / dom_avg_s
         fp64 = {"bound": "fp64 pipe", "achieved_gops": rate64 / 1e9, "peak_gops": peak64 / 1e9,
                 "frac": rate64 / peak64, "ops_per_cell": JACOBI_FP64_OPS,
                 "peak_source": "32-addition FP64 probe sweep measured in this run (L2-resident 2048^2)"}
@@ -420,7 +425,9 @@ def gpu_bench(args, rank: int, world: int):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "traffic_source": traffic_src,
                      "peak_source": peak_src,
-                     "kernel": f"group {group} (site {dom_site})", "kernel_ms": dom_avg_s * 1e3,
+                     "kernel": f"group {group} (site {dom_site}"
+                               f"{', persistent loop: %d iterations per launch' % iters if loop else ''})",
+                     "kernel_ms": dom_avg_s * 1e3,
                      "kernel_share": sum(dom_ms) / total_prof, "algorithmic_bytes_per_launch": alg_bytes,
                      "fp64": fp64},
         "e2e": e2e,
@@ -468,6 +475,35 @@ def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
         out["fp64" if mode is None else mode] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms,
                                                  "value": SWEEPS_PER_STEP * n * n / (ms * 1e-3) / 1e9,
                                                  "unit": "GLUP/s"}
+    # algorithmic bytes per cell and step.  "sweep" counts every pressure iteration as one
+    # sweep without temporal reuse (50 FP64 Jacobi sweeps, or residual + 49 defect iterations +
+    # correction); "launch" counts what the launches of the mixed path must move at least: the
+    # residual, ceil(49 / temporal) defect launches (the first reads r32 and writes d (and the
+    # 16-bit r), the others read r and d and write d) and the correction (p in, d in, p out).
+    # The FP64 groups of the step (source b with the first p sweep; u, v) come from the module.
+    hbm, _ = peaks()
+    xgrid.init(precision="double", cacheroot=JIT_CACHE, opt_level=3)
+    kp = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
+    from xgrid_gb300.native import NativeKernel
+    kp.native = NativeKernel(kp)
+    mod = kp.native.module
+    outer = algorithmic_bytes(mod, 0) + algorithmic_bytes(mod, 2)
+    jac = algorithmic_bytes(mod, 1)
+    iters = 49
+    nl = -(-iters // max(1, temporal))
+    for mode in ("fp64", "fp32", "fp16", "bf16"):
+        o = out[mode]
+        if mode == "fp64":
+            sweep = launch = outer + 50 * jac
+        else:
+            es = 4 if mode == "fp32" else 2
+            sweep = outer + (jac + 4) + iters * 3 * es + (16 + es)
+            first = 4 + es + (es if es == 2 else 0)
+            launch = outer + (jac + 4) + first + (nl - 1) * 3 * es + (16 + es)
+        o["bytes_per_cell_step"] = {"sweep": sweep, "launch": launch}
+        o["sweep_gbs"] = sweep * n * n / (o["ms_per_step"] * 1e-3) / 1e9
+        o["launch_gbs"] = launch * n * n / (o["ms_per_step"] * 1e-3) / 1e9
+        o["launch_hbm_frac"] = o["launch_gbs"] / hbm
     for mode in ("fp32", "fp16", "bf16"):
         err = {}
         for g in "puv":

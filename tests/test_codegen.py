@@ -60,6 +60,37 @@ def test_mixed_loop_has_temporal_tma_kernel():
     assert "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes" in hdr
 
 
+def test_persistent_loop_kernel_for_in_place_loops():
+    """The cavity pressure loop (implicit Jacobi sweep + four boundary sweeps) gets
+    a persistent loop launch: a cooperative launch, the grid barrier between
+    iterations, level and scratch alternating by iteration parity; a loop whose
+    body uses the loop variable or writes two grids does not."""
+    m = _gen(workloads.cavity_kernel, persistent=True)
+    assert "xgk_cavity_kernel_1_loop" in m.source
+    assert "cudaLaunchAttributeCooperative" in m.source
+    assert "xg_grid_sync(p.sync" in m.source and "xg_grid_exit(p.sync" in m.source
+    assert "(xg_it & 1) ? p.b1_0_1 : p.b1_0_0" in m.source
+    assert m.source.count("_loop(xg_G, &xg_h, xg_K, xg_s)") == 1
+    off = _gen(workloads.cavity_kernel)
+    assert "_loop(" not in off.source
+    nofuse = _gen(workloads.cavity_kernel, persistent=True, fuse=False)
+    assert "_loop(" not in nofuse.source
+
+    @xgrid.kernel()
+    def uses_counter(p: xgrid.grid[float, 2], n: int) -> None:
+        for i in range(0, n):
+            p[0, 0] = 0.25 * (p[1, 0][0] + p[-1, 0][0] + p[0, 1][0] + p[0, -1][0]) if i > 2 else p[0, 1][0]
+
+    @xgrid.kernel()
+    def two_grids(p: xgrid.grid[float, 2], q: xgrid.grid[float, 2], n: int) -> None:
+        for _ in range(0, n):
+            p[0, 0] = 0.25 * (p[1, 0][0] + p[-1, 0][0] + p[0, 1][0] + p[0, -1][0])
+            q[0, 0] = p[0, 0][0]
+
+    for k in (uses_counter, two_grids):
+        assert "_loop(xg_G" not in _gen(k, persistent=True).source
+
+
 def test_affine_degree():
     xgrid.init(precision="double", cacheroot="/tmp/xgcg", opt_level=3)
     defn = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel").ir

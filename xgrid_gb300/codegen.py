@@ -153,6 +153,7 @@ class CudaGenerator:
         self.mixed_slots: dict = {}   # grid slot -> aux bytes per cell of mixed-precision loops
         self.group_emitters: list = []
         self._plans: dict = {}
+        self.loop_groups: list = []   # groups with a persistent loop launch
         self.slots = analysis.grid_slots(self.defn)
         self.grid_names = {name: i for name, i in self.slots.items()}
         self.mode = OVERSTEP[config.overstep]
@@ -352,6 +353,8 @@ class CudaGenerator:
                 self.sweeps.extend(plan.group.sweeps)
                 self.mixed_slots[plan.slot] = mixed.AUX_BYTES_PER_CELL
                 MixedLoopEmitter(self, plan).emit(env, indent, out)
+            elif isinstance(s, ir.For) and self.loop_plan(s) is not None:
+                self.emit_loop(s, env, indent, out)
             elif isinstance(s, ir.For):
                 v = s.variable.name
                 out.append(f"{indent}for ({v} = {self.expr(s.start, env)}; {v} < {self.expr(s.end, env)}; "
@@ -372,6 +375,84 @@ class CudaGenerator:
                 plan = None
             self._plans[id(loop)] = plan
         return self._plans[id(loop)]
+
+    def loop_plan(self, loop: ir.For):
+        """The launch group of an in-place loop that runs as one persistent launch, or None.
+
+        The loop qualifies when its body is one implicit main sweep of a grid
+        followed by boundary sweeps of that grid (all at the cell itself, level
+        0), nothing in it depends on the loop variable, the sweeps form one
+        fusable launch group and every load of the rewritten grid reads level 0:
+        each iteration is then the same launch with the level and the scratch
+        buffer exchanged."""
+        if not (self.cfg.persistent and self.cfg.fuse) or not loop.body:
+            return None
+        key = ("loop", id(loop))
+        if key in self._plans:
+            return self._plans[key]
+        self._plans[key] = None
+        body = loop.body
+        if not all(isinstance(s, ir.Assignment) and isinstance(s.terminal, ir.Stencil) for s in body):
+            return None
+        names = {s.terminal.variable.name for s in body}
+        if len(names) != 1:
+            return None
+        target = names.pop()
+        uses = lambda node: any(isinstance(x, ir.Identifier) and x.variable.name == loop.variable.name
+                                for x in ir.walk(node))
+        for i, st in enumerate(body):
+            t = st.terminal
+            if t.time_offset != 0 or any(t.space_offset) or (i == 0) != (t.boundary_mask == 0) or uses(st.value):
+                return None
+        sweeps = [analysis.collect_sweep(st, self.slots, self.logger) for st in body]
+        if not sweeps[0].implicit or any(sw.implicit for sw in sweeps[1:]):
+            return None
+        slot = self.slots[target]
+        for sw in sweeps:
+            if any(st.variable.name == target and st.time_offset != 0 for st, _ in sw.loads):
+                return None
+        counter = [self.group_counter[0]]
+        groups = analysis.build_groups(sweeps, counter, True)
+        if len(groups) != 1 or not groups[0].fusable or groups[0].sweeps[0] is not sweeps[0]:
+            return None
+        if any(sw.write_version != 1 for sw in sweeps) or sweeps[0].read_version_of_target != 0:
+            return None
+        self._plans[key] = (slot, groups[0])
+        return self._plans[key]
+
+    def emit_loop(self, loop: ir.For, env, indent: str, out: list) -> None:
+        """Host block of a persistent loop: count the iterations as the loop
+        would (leaving the loop variable at its final value), run them in one
+        launch, else (launch not applicable) one group launch per iteration."""
+        slot, group = self.loop_plan(loop)
+        for sw in group.sweeps:
+            for st, _ in sw.loads:
+                self.depth = max(self.depth, abs(st.time_offset))
+            self.depth = max(self.depth, sw.level)
+        self.sweeps.extend(group.sweeps)
+        gid = group.index
+        self.group_counter[0] = gid + 1
+        em = SweepGroupEmitter(self, group)
+        dim = self.defn.signature.arguments[em.arg_index(slot)][1].dimension
+        self.group_tiling[gid] = DEFAULT_TILING[dim]
+        em.prepare()
+        n, v = self.op.name, loop.variable.name
+        out.append(f"{indent}{{")
+        out.extend(em.host_hoists(env, indent + "  "))
+        out.append(f"{indent}  int64_t xg_K = 0;")
+        out.append(f"{indent}  for ({v} = {self.expr(loop.start, env)}; {v} < {self.expr(loop.end, env)}; "
+                   f"{v} += {self.expr(loop.step, env)}) ++xg_K;")
+        out.append(f"{indent}  if (xg_K > 0) {{")
+        out.append(f"{indent}    const int xg_r = xg_fuse_{n} ? xgl_{n}_{gid}_loop(xg_G, &xg_h, xg_K, xg_s) : 0;")
+        out.append(f"{indent}    if (xg_r < 0) return xg_r;")
+        out.append(f"{indent}    if (xg_r == 0) for (int64_t xg_i = 0; xg_i < xg_K; ++xg_i) "
+                   f"XG_TRY(xgl_{n}_{gid}(xg_G, &xg_h, xg_s));")
+        out.append(f"{indent}  }}")
+        out.append(f"{indent}}}")
+        em.emit_kernels()
+        em.emit_loop()
+        self.group_emitters.append(em)
+        self.loop_groups.append(gid)
 
     # ================================================================ sweeps
     def emit_run(self, run: list, env, indent: str, out: list) -> None:
@@ -472,6 +553,20 @@ class CudaGenerator:
         src.append("  return 0;")
         src.append("}")
         src.append(f'extern "C" int xg_mixed_{name}(int64_t every) {{ xg_mixed_every_{name} = every; return 0; }}')
+        # error word of the persistent loops' grid barriers (1: a barrier wait gave up, the
+        # results of that call are invalid); clear = 1 also resets the barrier words
+        src.append(f'extern "C" int xg_loop_error_{name}(int clear) {{')
+        src.append("  int e = 0;")
+        for gid in self.loop_groups:
+            src += ["  {", "    unsigned w[2] = {0u, 0u};",
+                    f"    if (cudaMemcpyFromSymbol(w, xg_sync_{name}_{gid}, sizeof w) != cudaSuccess) return -1;",
+                    "    if (w[1]) e = 1;",
+                    "    if (clear && w[1]) {", "      const unsigned z[2] = {0u, 0u};",
+                    f"      if (cudaMemcpyToSymbol(xg_sync_{name}_{gid}, z, sizeof z) != cudaSuccess) return -1;",
+                    "    }", "  }"]
+        src.append("  (void)clear;")
+        src.append("  return e;")
+        src.append("}")
         implicit = sorted({s.slot for s in self.sweeps if s.implicit})
         if getattr(self.op, "noalloc", False) and grid_args and implicit:
             src.extend(self.noalloc_entry(name, entry, grid_args, implicit))
@@ -1256,9 +1351,26 @@ class SweepGroupEmitter:
         out.append(f"{indent}}}")
         return out
 
-    def main_kernel(self, tag: str, mains: list, bnd_phases: list, final=None) -> str:
+    def loop_locals(self, sweeps) -> list:
+        """Buffer pointers of the persistent loop kernel: the level and the scratch
+        buffer of the implicit sweep change roles every iteration (plain pointers,
+        no __restrict__, so no load takes the read-only path); the others are
+        read-only for the whole launch."""
+        out = []
+        for b in self.buffers(sweeps):
+            if b[0] == self.g.sweeps[0].slot and b[1] == self.g.sweeps[0].level:
+                other = (b[0], b[1], 1 - b[2])
+                out.append(f"  {self.elem(b[0])}* {self.bname(b)} = (xg_it & 1) ? p.{self.bname(other)} : "
+                           f"p.{self.bname(b)};")
+            else:
+                out.append(f"  {self.elem(b[0])}* __restrict__ {self.bname(b)} = p.{self.bname(b)};")
+        return out
+
+    def main_kernel(self, tag: str, mains: list, bnd_phases: list, final=None, loop: bool = False) -> str:
         """Tile kernel: main sweeps ``mains`` (indices into the group) then the
-        boundary phases ``bnd_phases`` on the tile's own cells."""
+        boundary phases ``bnd_phases`` on the tile's own cells.  ``loop``: the
+        persistent variant, p.K iterations of the group in one cooperative launch
+        (tiles strided over the CTAs, a grid barrier between iterations)."""
         n, gid = self.name, self.gid
         sweeps = [self.g.sweeps[j] for j in mains]
         # neighbourhood of the main loads, for the unchecked fast path
@@ -1272,8 +1384,16 @@ class SweepGroupEmitter:
         zm = self.zmarch_ok(mains, bnd_phases)
         blocks = ZWALK_BLOCKS if zm else self.min_blocks()  # the z walk keeps several planes in registers
         lines = [f"template <typename I> __global__ void __launch_bounds__(256, {blocks}) xgk_{n}_{gid}_{tag}("
-                 f"const __grid_constant__ struct xgp_{n}_{gid}_{tag} p) {{"] + TILE_PROLOGUE + \
-            self.restrict_locals([self.g.sweeps[j] for j in list(mains) + list(bnd_phases)]) + [
+                 f"const __grid_constant__ struct xgp_{n}_{gid}_{tag} p) {{"]
+        members = [self.g.sweeps[j] for j in list(mains) + list(bnd_phases)]
+        if loop:
+            lines += ["  for (int xg_it = 0; xg_it < (int)p.K; ++xg_it) {",
+                      "  for (int xg_tt = blockIdx.x; xg_tt < (int)(p.ntz * p.nty * p.ntx); xg_tt += gridDim.x) {",
+                      "  const xg_tile T = xg_tile_at(xg_tt, p.Z, p.Y, p.X, p.tz, p.ty, p.tx, p.nty, p.ntx, p.ntz);"]
+            lines += TILE_PROLOGUE[1:] + self.loop_locals(members)
+        else:
+            lines += TILE_PROLOGUE + self.restrict_locals(members)
+        lines += [
                  f"  const bool fast = p.same && z0 + ({lo[0]}) >= 0 && z1 - 1 + ({hi[0]}) < p.Z && "
                  f"y0 + ({lo[1]}) >= 0 && y1 - 1 + ({hi[1]}) < p.Y && x0 + ({lo[2]}) >= 0 && x1 - 1 + ({hi[2]}) < p.X;"]
         mask_vars = {}
@@ -1336,6 +1456,11 @@ class SweepGroupEmitter:
             lines += ["    " + l for l in body]
             lines.append("  }}")
             lines += ["  " + l for l in post]
+        if loop:
+            lines += ["  }",
+                      "  if (xg_it + 1 < p.K && !xg_grid_sync(p.sync, gridDim.x, (unsigned)(xg_it + 1))) return;",
+                      "  }",
+                      "  xg_grid_exit(p.sync, gridDim.x, (unsigned)(p.K - 1));"]
         lines.append("}")
         return "\n".join(lines)
 
@@ -1494,6 +1619,88 @@ class SweepGroupEmitter:
                 L.append(f"  {{ void* t_ = G[{s.slot}].level[{s.level}]; G[{s.slot}].level[{s.level}] = "
                          f"G[{s.slot}].scratch; G[{s.slot}].scratch = t_; }}")
         L += ["  return 1;", "}"]
+        self.gen.host_chunks.append("\n".join(L))
+
+
+    def emit_loop(self) -> None:
+        """Persistent launch of ``K`` iterations of this group (the body of an
+        in-place loop): the fused kernel's tile work in a loop over iterations,
+        one cooperative launch of at most the resident CTAs, a grid barrier
+        between iterations.  The launcher returns 1 when it ran, 0 when the
+        launch does not apply (shapes, tile-local boundary reads), so the caller
+        falls back to one launch per iteration."""
+        n, gid = self.name, self.gid
+        sweeps = self.g.sweeps
+        mains = [j for j, s in enumerate(sweeps) if s.is_main]
+        bnds = [j for j, s in enumerate(sweeps) if not s.is_main]
+        extra = ["int64_t K", "unsigned* sync"]
+        for j in mains:
+            extra += [f"const int32_t* m{j}", f"const uint8_t* tzero{j}"]
+        for j in bnds:
+            extra += [f"const int32_t* bo{j}", f"const int64_t* bc{j}"]
+        self.gen.device_chunks.append(f"__device__ unsigned xg_sync_{n}_{gid}[2] = {{0u, 0u}};")
+        self.gen.device_chunks.append(self.params_struct("loop", sweeps, extra))
+        self.gen.device_chunks.append(self.main_kernel("loop", mains, bnds, loop=True))
+        dom = sweeps[mains[0]].slot
+        s0 = sweeps[0]
+        L = [f"static int xgl_{n}_{gid}_loop(xg_grid* G, const struct xgh_{n}_{gid}* h, int64_t K, cudaStream_t s) {{"]
+        L += self.check_levels(sweeps)
+        L += self.fill_params("loop", sweeps, dom)
+        for j in mains + bnds:
+            L.append(f"  if (!xg_same_ext(xg_extent(&G[{sweeps[j].slot}]), dom)) return 0;")
+        L.append("  int64_t ntiles = 0;")
+        for j in mains:
+            sj = sweeps[j]
+            L += [f"  p.m{j} = xg_mask_device(G[{sj.slot}].mask);",
+                  f"  XG_TRY(xg_mask_tiles(G[{sj.slot}].mask, tl, 0, &p.tzero{j}, NULL, NULL, &ntiles));"]
+        for j in bnds:
+            sj = sweeps[j]
+            L.append(f"  XG_TRY(xg_mask_tiles(G[{sj.slot}].mask, tl, {sj.mask}, NULL, &p.bo{j}, &p.bc{j}, &ntiles));")
+        for j, offs in self.g.local_checks:
+            sj = sweeps[j]
+            flat = ", ".join(str(v) for o in offs for v in o)
+            L += ["  {", f"    static const int32_t offs[] = {{{flat}}};", "    int ok = 0;",
+                  f"    XG_TRY(xg_mask_tile_local(G[{sj.slot}].mask, tl, {sj.mask}, {len(offs)}, offs, "
+                  f"xg_overstep, &ok));",
+                  "    if (!ok) return 0;", "  }"]
+        L += ["  if (ntiles != p.ntz * p.nty * p.ntx) XG_FAIL(\"tile table mismatch\");",
+              "  if (K > 0x7fffffffLL || ntiles > 0x7fffffffLL) return 0;",
+              "  p.K = K;",
+              f"  XG_CUDA(cudaGetSymbolAddress((void**)&p.sync, xg_sync_{n}_{gid}));",
+              "  const dim3 block(tl[3], tl[4], tl[5]);",
+              "  const int threads = tl[3] * tl[4] * tl[5];",
+              "  const bool small = xg_small_index(p.Z, p.Y, p.X);",
+              "  int per_sm = 0;",
+              f"  if (small) XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xgk_{n}_{gid}_loop<int>, "
+              "threads, 0));",
+              f"  else XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xgk_{n}_{gid}_loop<int64_t>, "
+              "threads, 0));",
+              "  int dev = 0, sms = 0;",
+              "  XG_CUDA(cudaGetDevice(&dev));",
+              "  XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));",
+              "  if (per_sm < 1) return 0;",
+              "  const int64_t resident = (int64_t)per_sm * sms;",
+              "  const int64_t nb = ntiles < resident ? ntiles : resident;",
+              "  if (nb < 1) return 0;",
+              "  cudaLaunchConfig_t lc;",
+              "  memset(&lc, 0, sizeof lc);",
+              "  cudaLaunchAttribute at[1];",
+              "  at[0].id = cudaLaunchAttributeCooperative;",
+              "  at[0].val.cooperative = 1;",
+              "  lc.gridDim = dim3((unsigned)nb, 1, 1);",
+              "  lc.blockDim = block;",
+              "  lc.dynamicSmemBytes = 0;",
+              "  lc.stream = s;",
+              "  lc.attrs = at;",
+              "  lc.numAttrs = 1;",
+              f"  xg_prof_launch({gid * 64 + 61}, s);",
+              f"  if (small) XG_CUDA(cudaLaunchKernelEx(&lc, xgk_{n}_{gid}_loop<int>, p));",
+              f"  else XG_CUDA(cudaLaunchKernelEx(&lc, xgk_{n}_{gid}_loop<int64_t>, p));",
+              f"  xg_prof_end({gid * 64 + 61}, s);",
+              # K exchanges of level and scratch: the parity of K decides which buffer holds the result
+              f"  if (K & 1) {{ void* t_ = G[{s0.slot}].level[{s0.level}]; G[{s0.slot}].level[{s0.level}] = "
+              f"G[{s0.slot}].scratch; G[{s0.slot}].scratch = t_; }}",
+              "  return 1;", "}"]
         self.gen.host_chunks.append("\n".join(L))
 
 

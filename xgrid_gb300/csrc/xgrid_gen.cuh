@@ -358,6 +358,66 @@ __device__ __forceinline__ bool xg_mbar_wait(uint64_t* bar, unsigned parity, uns
 }
 
 // ---------------------------------------------------------------------------
+// Persistent loop kernels: one cooperative launch runs K iterations of a launch
+// group, each CTA walking the tiles blockIdx.x, blockIdx.x + gridDim.x, ... and
+// all CTAs meeting at a grid barrier between iterations.
+
+// Tile number t of a (ntz, nty, ntx) tiling, numbered like xg_tile_of.
+__device__ __forceinline__ xg_tile xg_tile_at(int64_t t, int64_t Z, int64_t Y, int64_t X, int tz, int ty, int tx,
+                                              int64_t nty, int64_t ntx, int64_t ntz) {
+  xg_tile T;
+  const int ix = (int)(t % ntx), iy = (int)((t / ntx) % nty), iz = (int)(t / (ntx * nty));
+  T.t = t;
+  T.x0 = ix * tx;
+  T.x1 = (ix == ntx - 1) ? (int)X : (ix + 1) * tx;
+  T.y0 = iy * ty;
+  T.y1 = (iy == nty - 1) ? (int)Y : (iy + 1) * ty;
+  T.z0 = iz * tz;
+  T.z1 = (iz == ntz - 1) ? (int)Z : (iz + 1) * tz;
+  return T;
+}
+
+// Grid barrier number `gen` (1, 2, ...) of a cooperative launch of `nblocks` CTAs.
+// sync[0] counts arrivals (zero at launch); barrier `gen` is complete when it
+// reaches gen * nblocks.  Thread 0 of each CTA arrives with a release and polls
+// with acquires, so the writes of every CTA before the barrier are visible to
+// every CTA after it.  The poll is bounded: after XG_WAIT_LIMIT polls it sets
+// the error word sync[1] and the CTA leaves (false).
+__device__ __forceinline__ bool xg_grid_sync(unsigned* sync, unsigned nblocks, unsigned gen) {
+  __shared__ int ok_;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+    const unsigned target = gen * nblocks;
+    __threadfence();
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(sync), "r"(1u) : "memory");
+    int ok = 0;
+    for (unsigned i = 0; i < XG_WAIT_LIMIT; ++i) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(sync) : "memory");
+      if ((int)(v - target) >= 0) {
+        ok = 1;
+        break;
+      }
+    }
+    if (!ok) atomicExch((int*)(sync + 1), 1);
+    __threadfence();
+    ok_ = ok;
+  }
+  __syncthreads();
+  return ok_ != 0;
+}
+
+// Last arrival of a launch that passed `barriers` grid barriers: the CTA whose
+// arrival completes the count puts it back to zero for the next launch (every
+// CTA has left its last poll by then).
+__device__ __forceinline__ void xg_grid_exit(unsigned* sync, unsigned nblocks, unsigned barriers) {
+  if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+    const unsigned old = atomicAdd(sync, 1u);
+    if (old + 1u == (barriers + 1u) * nblocks) atomicExch(sync, 0u);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Power-of-two storage scales of 16-bit fields.  For a field whose largest
 // magnitude is m, xg_scale_exp(m, A) = A - floor(log2 m) (clamped to the normal
 // exponent range), so m * 2^s lies in [2^A, 2^(A+1)); multiplying by 2^s and by

@@ -66,6 +66,18 @@ class NativeKernel:
         self.mixed_fn(int(every))
         runtime.load().xg_graph_clear(self.fn_ptr)
 
+    def loop_error(self, clear: bool = False) -> int:
+        """1 when a grid-barrier wait of a persistent loop launch gave up (the
+        results of that call are invalid), else 0; ``clear`` resets the word.
+        Synchronises with the device."""
+        fn = getattr(self.lib.dylib, f"xg_loop_error_{self.module.name}")
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.c_int]
+        rc = fn(1 if clear else 0)
+        if rc < 0:
+            self.logger.dead("reading the persistent-loop error word failed")
+        return rc
+
     # ---------------------------------------------------------------- tuning
     def set_tiling(self, group: int, tiling: tuple) -> None:
         """(tz, ty, tx, block.x, block.y, block.z) for one launch group."""
