@@ -621,7 +621,7 @@ def adjoint_section(n: int, steps: int, every: int, torch_n: int) -> dict:
         torch.cuda.synchronize()
         s.synchronize()
         t2 = time.perf_counter()
-        return t1 - t0, t2 - t1, float(loss)
+        return t1 - t0, t2 - t1, float(loss.detach())
 
     f, bwd, loss = run_ours(n, steps)
     cells = n ** 3

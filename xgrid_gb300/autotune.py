@@ -167,6 +167,27 @@ def tune_batch(native, problems, candidates=None) -> tuple:
 
 
 # ------------------------------------------------------------ single calls
+def balanced_candidates(shape, sms: int) -> list:
+    """2-D tilings whose number of full tiles is a whole number of waves: k x SMs x
+    (4 or 6 resident CTAs per SM, the FP64 and FP32 tile kernels' occupancies).
+    Power-of-two tiles of a 2^n + 1 grid give 2^m full tiles, which never fill
+    152 x 4 slots (1025^2 with 64 x 32 tiles: 512 tiles, 84 % of one wave)."""
+    if len(shape) != 2 or sms <= 0:
+        return []
+    Y, X = shape
+    out = []
+    for per_sm in (4, 6):
+        for tx in (32, 64):
+            nx = max(1, X // tx)
+            for k in (1, 2, 3):
+                nty = max(1, (k * sms * per_sm) // nx)
+                ty = -(-Y // nty)
+                c = (1, ty, tx, 32, 8, 1)
+                if 8 <= ty <= 256 and c not in out:
+                    out.append(c)
+    return out
+
+
 def group_candidates(ndim: int) -> list:
     """(tz, ty, tx, block.x, block.y, block.z) candidates of a launch group."""
     if ndim == 1:
@@ -202,6 +223,12 @@ def tune(op, *args, calls: int = 2) -> dict:
             nk.set_tiling(g, t)
         return chosen
     ndim = max(len(g.shape) for g in grids)
+    t = device.torch()
+    sms = t.cuda.get_device_properties(t.cuda.current_device()).multi_processor_count
+    cands = group_candidates(ndim)
+    if ndim == 2:
+        cands += [c for c in balanced_candidates(max((g.shape for g in grids), key=lambda s: s[0] * s[1]), sms)
+                  if c not in cands]
     snap = Snapshot(grids)
     chosen = {}
 
@@ -212,7 +239,7 @@ def tune(op, *args, calls: int = 2) -> dict:
         for g in groups:
             base = nk._tiling_key(g)
             results = []
-            for c in [base] + [c for c in group_candidates(ndim) if c != base]:
+            for c in [base] + [c for c in cands if c != base]:
                 nk.set_tiling(g, c)
                 try:
                     results.append((_time(run), c))
