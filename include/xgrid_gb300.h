@@ -169,6 +169,14 @@ int xg_call(xg_entry_fn fn, xg_grid* grids, int ngrids, const void* args, size_t
 int xg_graph_clear(xg_entry_fn fn);
 int64_t xg_graph_count(void);
 
+/* ---- host mirror copies --------------------------------------------------- */
+/* Asynchronous copy of `bytes` on `stream` between a grid level and its
+ * page-locked host mirror (either direction; cudaMemcpyAsync with the direction
+ * inferred from the pointers).  Carries the numpy <-> device transfers behind
+ * Grid.now / Grid._data and the upload before a call (the reference hands its
+ * numpy levels to the C code directly, xgrid/xgrid/__init__.py:60-68). */
+int xg_memcpy(void* dst, const void* src, size_t bytes, void* stream);
+
 /* ---- launch accounting (used by generated modules and the benchmark) ----- */
 /* Generated modules call xg_prof_launch() before every kernel launch and
  * xg_prof_end() after it.  Both only count unless profiling is on; with

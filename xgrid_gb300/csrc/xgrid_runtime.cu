@@ -651,6 +651,13 @@ cudaEvent_t pooled_event() {
 }
 }  // namespace
 
+int xg_memcpy(void* dst, const void* src, size_t bytes, void* stream) {
+  if (bytes == 0) return 0;
+  if (!dst || !src) return fail("xg_memcpy: null pointer");
+  XG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, static_cast<cudaStream_t>(stream)));
+  return 0;
+}
+
 void xg_prof_enable(int on) {
   std::lock_guard<std::mutex> lock(g_prof_mu);
   g_prof_on = on;

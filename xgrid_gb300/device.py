@@ -9,6 +9,8 @@ from __future__ import annotations
 import numpy as np
 
 _stream = None
+_handle = None
+_cuda_ok = False
 
 
 def torch():
@@ -17,8 +19,13 @@ def torch():
 
 
 def require_cuda() -> None:
+    global _cuda_ok
+    if _cuda_ok:
+        return
     t = torch()
-    if not t.cuda.is_available():
+    if t.cuda.is_available():
+        _cuda_ok = True  # a device that was visible stays visible for the process
+    else:
         raise Exception("xgrid: no CUDA device is visible; the GB300 backend runs every sweep on the GPU "
                         "and has no CPU fallback")
 
@@ -33,7 +40,17 @@ def stream():
 
 
 def stream_handle() -> int:
-    return stream().cuda_stream
+    global _handle
+    if _handle is None:
+        _handle = stream().cuda_stream
+    return _handle
+
+
+def copy_async(dst: int, src: int, nbytes: int) -> None:
+    """Asynchronous copy on the backend stream between device memory and
+    page-locked host memory (addresses as integers)."""
+    from . import runtime
+    runtime.check(runtime.load().xg_memcpy(dst, src, nbytes, stream_handle()), "copy")
 
 
 def synchronize() -> None:

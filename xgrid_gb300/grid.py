@@ -124,7 +124,8 @@ class Grid:
 
     def tensor(self, level: int = 0):
         """Device view of a level as a torch tensor of the grid's shape."""
-        self._sync_device(False)
+        if self._sync_device(False):
+            device.stream().synchronize()  # uploads done before any stream uses the view
         dt = device.torch_dtype(self.numpy_dtype)
         if dt is None:
             self.logger.dead("tensor() is only available for numeric grids")
@@ -139,13 +140,8 @@ class Grid:
             if lv.auth == "zero":
                 lv.auth = "host"
         if lv.auth == "dev":
-            s = device.stream()
-            t = device.torch()
-            src = lv.dev[: self._nbytes]
-            dst = t.from_numpy(lv.host.reshape(-1).view(np.uint8))
-            with t.cuda.stream(s):
-                dst.copy_(src, non_blocking=True)
-            s.synchronize()
+            device.copy_async(lv.host.ctypes.data, lv.dev.data_ptr(), self._nbytes)
+            device.stream().synchronize()
             lv.auth = "both"
         if dirty:
             lv.auth = "host"
@@ -156,8 +152,6 @@ class Grid:
         uploaded (the caller then waits for the copies before returning, so the
         host arrays handed out earlier can be modified again safely)."""
         device.require_cuda()
-        t = device.torch()
-        s = device.stream()
         uploaded = False
         for lv in self._levels:
             if lv.dev is None:
@@ -165,9 +159,9 @@ class Grid:
                 if lv.auth == "zero":
                     lv.auth = "dev"
             if lv.auth == "host":
-                src = t.from_numpy(np.ascontiguousarray(lv.host).reshape(-1).view(np.uint8))
-                with t.cuda.stream(s):
-                    lv.dev[: self._nbytes].copy_(src, non_blocking=True)
+                if not lv.host.flags.c_contiguous:
+                    lv.host = np.ascontiguousarray(lv.host)
+                device.copy_async(lv.dev.data_ptr(), lv.host.ctypes.data, self._nbytes)
                 lv.auth = "both"
                 uploaded = True
         if need_scratch and self._scratch is None:

@@ -120,8 +120,12 @@ class NativeKernel:
         for i, g in enumerate(grids):
             aux = mixed.aux_bytes(g.shape) if i in self.module.aux_per_cell else 0
             uploaded |= g._sync_device(i in self.scratch_slots, aux)
+        copied = None
         if uploaded:
-            device.stream().synchronize()
+            # the launch follows the uploads on the stream; the host arrays may be
+            # modified again once the copies (not the launch) are done
+            copied = self._upload_event()
+            copied.record(device.stream())
         packed = self.pack(values)
         arr = (runtime.XGGrid * max(len(grids), 1))(*[g.serialize() for g in grids])
         ret = self.ret_type.ctype() if self.ret_type is not None else None
@@ -131,6 +135,8 @@ class NativeKernel:
                                     ctypes.cast(ctypes.byref(ret), ctypes.c_void_p) if ret is not None else None,
                                     ctypes.sizeof(ret) if ret is not None else 0,
                                     device.stream_handle(), 1 if self.use_graph else 0)
+        if copied is not None:
+            copied.synchronize()
         if rc != 0:
             self.logger.dead(f"kernel '{self.module.name}' failed: {runtime.last_error()}")
         for g, st in zip(grids, arr):
@@ -140,6 +146,12 @@ class NativeKernel:
         if isinstance(self.ret_type, Structure):
             return self.ret_type.deserialize(ret)
         return self.ret_type.deserialize(ret.value)
+
+    def _upload_event(self):
+        ev = getattr(self, "_uploaded", None)
+        if ev is None:
+            ev = self._uploaded = device.torch().cuda.Event()
+        return ev
 
     def pack(self, values: list):
         packed = self.args_type()
