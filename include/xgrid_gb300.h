@@ -177,6 +177,14 @@ int64_t xg_graph_count(void);
  * numpy levels to the C code directly, xgrid/xgrid/__init__.py:60-68). */
 int xg_memcpy(void* dst, const void* src, size_t bytes, void* stream);
 
+/* ---- index width ----------------------------------------------------------- */
+/* Every tile kernel exists for 32-bit and 64-bit linear indices; the 64-bit one
+ * runs for grids of 2^31 cells or more.  xg_force_wide_index(1) makes every
+ * later launch take the 64-bit kernels (a test switch: the two must give the
+ * same bits; cached CUDA graphs keep the kernels they captured). */
+void xg_force_wide_index(int on);
+int xg_wide_index_forced(void);
+
 /* ---- launch accounting (used by generated modules and the benchmark) ----- */
 /* Generated modules call xg_prof_launch() before every kernel launch and
  * xg_prof_end() after it.  Both only count unless profiling is on; with

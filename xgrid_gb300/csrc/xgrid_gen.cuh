@@ -273,8 +273,11 @@ __device__ __forceinline__ xg_tile xg_tile_of(int64_t Z, int64_t Y, int64_t X, i
 }
 
 // Tile kernels are instantiated for int and int64_t linear indices; the 32-bit
-// one (fewer integer instructions per load) runs when every index fits.
-static inline bool xg_small_index(int64_t Z, int64_t Y, int64_t X) { return Z * Y * X < (1LL << 31) - 1; }
+// one (fewer integer instructions per load) runs when every index fits and the
+// runtime's test switch (xg_force_wide_index) is off.
+static inline bool xg_small_index(int64_t Z, int64_t Y, int64_t X) {
+  return Z * Y * X < (1LL << 31) - 1 && !xg_wide_index_forced();
+}
 
 // Launch grid of a tiling; fails when an axis exceeds what CUDA allows.
 static inline int xg_tile_grid(int64_t ntx, int64_t nty, int64_t ntz, dim3* grid) {

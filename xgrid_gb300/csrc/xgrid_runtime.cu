@@ -651,6 +651,14 @@ cudaEvent_t pooled_event() {
 }
 }  // namespace
 
+namespace {
+std::atomic<int> g_wide_index{0};
+}
+
+void xg_force_wide_index(int on) { g_wide_index.store(on ? 1 : 0); }
+
+int xg_wide_index_forced(void) { return g_wide_index.load(std::memory_order_relaxed); }
+
 int xg_memcpy(void* dst, const void* src, size_t bytes, void* stream) {
   if (bytes == 0) return 0;
   if (!dst || !src) return fail("xg_memcpy: null pointer");

@@ -61,6 +61,8 @@ SIGNATURES = {
     "xg_call": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(XGGrid), ctypes.c_int, ctypes.c_void_p,
                                ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int]),
     "xg_memcpy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "xg_force_wide_index": (None, [ctypes.c_int]),
+    "xg_wide_index_forced": (ctypes.c_int, []),
     "xg_graph_clear": (ctypes.c_int, [ctypes.c_void_p]),
     "xg_graph_count": (ctypes.c_int64, []),
     "xg_prof_enable": (None, [ctypes.c_int]),
