@@ -3,7 +3,7 @@
 The defect iteration ``d <- L(d) + r`` of ``xgrid_gb300.mixed`` runs ``T``
 iterations per launch instead of one.  Each CTA owns a tile of ``TY x TX``
 cells and works on a *box*: the tile plus a halo of ``HY = T * sy`` rows and
-``HX = roundup(T * sx, 8)`` columns per side (``sy, sx``: reach of the loop
+``HX = roundup(T * sx, 16 bytes / element)`` columns per side (``sy, sx``: reach of the loop
 body's main sweep).  Per launch:
 
 1. one thread stages the box of ``d`` and of ``r`` into shared memory with two
@@ -66,6 +66,9 @@ class TemporalDefect:
         self.dim = gen.defn.scope[plan.target].type.dimension
         self.dt, self.kind, self.cutype = STORAGE[gen.cfg.mixed]
         self.scaled = self.kind != 0
+        # a TMA box must start on a 16-byte boundary: the x halo is a multiple of 4 FP32 or
+        # 8 16-bit elements, so that every box's first column (tile origin - halo) is one
+        self.xalign = 4 if self.kind == 0 else 8
         self.main_offs = target_offsets(self.sweeps[0], self.slot)
         self.sy = max([abs(o[1]) for o in self.main_offs] + [0])
         self.sx = max([abs(o[2]) for o in self.main_offs] + [0])
@@ -263,7 +266,8 @@ class TemporalDefect:
              f"  *T = xg_mxt_{n}[0];",
              f"  *RS = xg_mxt_{n}[1];",
              "  if (*RS != 8 && *RS != 16 && *RS != 24) return 0;",
-             f"  halo[0] = 0; halo[1] = *T * {self.sy}; halo[2] = (*T * {self.sx} + 7) / 8 * 8;",
+             f"  halo[0] = 0; halo[1] = *T * {self.sy}; halo[2] = (*T * {self.sx} + {self.xalign - 1}) / "
+             f"{self.xalign} * {self.xalign};",
              f"  core[0] = 1; core[1] = 2 * *RS - 2 * halo[1]; core[2] = {BX} - 2 * halo[2];",
              "  if (core[1] < 1 || core[2] < 8) return 0;",
              f"  const int32_t shrink[3] = {{0, {self.sy}, {self.sx}}};"]
