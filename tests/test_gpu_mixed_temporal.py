@@ -109,12 +109,14 @@ def relax_column(p: xgrid.grid[float, 2], f: xgrid.grid[float, 2], iters: int) -
             p[0, 0] = 0.0
 
 
-@pytest.mark.parametrize("column,temporal_used", [(60, True), (118, False)])
+@pytest.mark.parametrize("column,temporal_used", [(60, True), (118, True), (122, False)])
 def test_box_check_accepts_and_rejects(cacheroot, column, temporal_used):
     """A column of boundary cells that copies its right neighbour: deep inside a box
-    the temporal path runs; at column 118 (next to the inner edge of the first box,
-    128 columns with a halo of 8) the copy would read a stale cell, the check refuses
-    and the loop runs one iteration per launch.  Same bits either way."""
+    (60), and at the last columns of the first tile (118: FP32 boxes are 128 columns
+    with a halo of 4, tiles 120 wide) the temporal path runs; at column 122 (two
+    columns from the first box's inner edge at 124) the copy would read a stale
+    cell, the check refuses and the loop runs one iteration per launch.  Same bits
+    either way."""
     xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3, mixed="fp32")
     k = Operator(relax_column.func, "kernel", "relax_column")
     from xgrid_gb300.native import NativeKernel
