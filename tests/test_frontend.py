@@ -126,3 +126,61 @@ def test_grid_api_on_host():
     assert g.dimension == 2 and g.boundary.dtype.name == "int32"
     g._op_invoke(3, True)
     assert g.time == 3
+
+
+@pytest.mark.parametrize("kw,msg", [
+    ({"overstep": "mirror"}, "Invalid overstep"),
+    ({"precision": "half"}, "Invalid precision"),
+    ({"mixed": "fp8"}, "Invalid mixed precision"),
+    ({"opt_level": 5}, "Invalid opt_level"),
+    ({"mixed_temporal": 17}, "Invalid mixed_temporal"),
+    ({"mixed_rows": 12}, "Invalid mixed_rows"),
+    ({"int_adds": -1}, "Invalid int_adds"),
+])
+def test_invalid_configuration_is_rejected(kw, msg):
+    with pytest.raises(Exception) as e:
+        xgrid.init(cacheroot="/tmp/xgfe", **kw)
+    assert msg in str(e.value)
+
+
+def test_configuration_defaults_and_flags():
+    from xgrid_gb300.config import get_config
+    xgrid.init(cacheroot="/tmp/xgfe")
+    c = get_config()
+    assert (c.precision, c.overstep, c.mixed, c.persistent, c.fuse, c.graph) == ("float", "none", None, False, True,
+                                                                                  True)
+    assert "--fmad=false" in c.nvcc_flags
+    xgrid.init(cacheroot="/tmp/xgfe", exact=False, precision="double", persistent=True)
+    c = get_config()
+    assert "--fmad=false" not in c.nvcc_flags and c.fsize == 8 and c.persistent
+
+
+@pytest.mark.parametrize("shape,msg", [((0, 4), "extents must be positive"), ((2, 2, 2, 2), "not supported")])
+def test_grid_shapes_rejected(shape, msg):
+    with pytest.raises(Exception) as e:
+        xgrid.Grid(shape, float)
+    assert msg in str(e.value)
+
+
+def test_grid_level_rotation_follows_the_reference():
+    """tick moves the last level to the front (xgrid/xgrid/__init__.py:49-54)."""
+    g = xgrid.Grid(5, float)
+    g._op_invoke(3, False)
+    for i in range(3):
+        g.fill(g.now * 0 + i, time=-i)
+    assert [float(g._data[i][0]) for i in range(3)] == [0.0, 1.0, 2.0]
+    g._op_invoke(3, True)
+    assert [float(g._data[i][0]) for i in range(3)] == [2.0, 0.0, 1.0]
+    # fill beyond the current depth extends the level list
+    g.fill(g.now * 0 + 7, time=4)
+    assert g.time == 5 and float(g._data[4][0]) == 7.0
+
+
+def test_grid_read_is_a_copy_and_now_is_the_level():
+    g = xgrid.Grid((3, 3), float)
+    g.now[...] = 2.0
+    r = g.read(0)
+    r[...] = 5.0
+    assert (g.now == 2.0).all()
+    g[1, 1] = 9.0
+    assert g.now[1, 1] == 9.0 and g[1, 1] == 9.0
