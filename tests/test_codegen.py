@@ -6,7 +6,7 @@ import pytest
 
 import xgrid
 import workloads
-from xgrid_gb300 import analysis, mixed
+from xgrid_gb300 import mixed
 from xgrid_gb300.codegen import CudaGenerator
 from xgrid_gb300.config import get_config
 from xgrid_gb300.operator import Operator

@@ -4,7 +4,6 @@ rendezvous and max-reduction run here with gloo on CPU, world size 2."""
 import os
 import socket
 
-import pytest
 import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp

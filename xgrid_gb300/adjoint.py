@@ -25,8 +25,6 @@ function of the previous state only.
 from __future__ import annotations
 
 import ctypes
-import dataclasses
-import hashlib
 
 from . import analysis, ir
 from .log import Logger

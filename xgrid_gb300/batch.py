@@ -25,7 +25,6 @@ have the same shape within a problem.
 from __future__ import annotations
 
 from . import analysis, ir
-from .types import GridType
 
 DEPTH_MAX = 8
 

@@ -38,7 +38,7 @@ import math
 from . import analysis, ir
 from .config import Configuration
 from .log import Logger
-from .types import (Boolean, Floating, GridType, Ignore, Integer, Pointer, Structure, Value,
+from .types import (Boolean, Floating, GridType, Ignore, Integer, Pointer, Structure,
                     Void)
 
 OVERSTEP = {"none": "XG_OVERSTEP_NONE", "limit": "XG_OVERSTEP_LIMIT", "wrap": "XG_OVERSTEP_WRAP"}

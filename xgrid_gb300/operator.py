@@ -9,12 +9,11 @@ for kernels that return a value.
 """
 from __future__ import annotations
 
-import ctypes
 from typing import Any, Callable
 
 from . import ir
 from .log import Logger
-from .types import BaseType, Void
+from .types import BaseType
 
 CustomTypecheck = Callable[[list], BaseType]
 
