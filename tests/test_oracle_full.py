@@ -1,0 +1,37 @@
+"""The C oracle at the benchmark programs' full sizes against the reference's
+own results, pinned as SHA-256 digests of every time level (recorded by
+``tests/golden/make_digests.py`` from the reference package): diffusion 512^2
+FP64 for 500 steps and the lid-driven cavity 1025^2 FP64 for 5 steps.  The GPU
+tests compare the GPU path with this oracle at the same sizes, so the chain GPU
+= oracle = reference holds at full size, not only on the small golden cases."""
+import hashlib
+import json
+import os
+
+import numpy as np
+
+from oracle import native
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+DIGESTS = json.load(open(os.path.join(HERE, "full_digests.json")))
+
+
+def _digests(levels):
+    return [hashlib.sha256(np.ascontiguousarray(x).tobytes()).hexdigest() for x in levels]
+
+
+def test_diffusion_512_500_steps_matches_reference_digests():
+    ref = DIGESTS["diffusion_512"]
+    field, c = native.diffusion_field(512, seed=0)
+    assert repr(c) == ref["c"]
+    native.Oracle("port").diffusion(field, c, 500)
+    assert _digests(field.levels) == ref["u"]
+
+
+def test_cavity_1025_5_steps_matches_reference_digests():
+    ref = DIGESTS["cavity_1025"]
+    n = 1025
+    f = native.cavity_fields(n)
+    native.Oracle("port").cavity(f, (1.0, 0.1, 1e-5, 2.0 / (n - 1), 2.0 / (n - 1)), 5)
+    for k in "bpuv":
+        assert _digests(f[k].levels) == ref[k], k
