@@ -133,3 +133,31 @@ def cavity_1025():
     for _ in range(5):
         cavity(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
     return {k: digests(g) for k, g in grids.items()}
+
+
+@full
+def convdiff_square():
+    """Square periodic FP32 convection-diffusion problems (the batched program's
+    stencil on grids the reference addresses correctly): 64^2, 257^2, 512^2,
+    coefficients from seed 5, 200 steps each."""
+    xgrid.init(cacheroot=CACHEROOT, opt_level=3, precision="float", overstep="wrap")
+
+    @xgrid.kernel()
+    def convdiff(u: xgrid.grid[float, 2], a0: float, axm: float, axp: float, aym: float, ayp: float) -> None:
+        u[0, 0] = a0 * u[0, 0] + axm * u[0, -1] + axp * u[0, 1] + aym * u[-1, 0] + ayp * u[1, 0]
+
+    rng = np.random.default_rng(5)
+    out = {}
+    for n in (64, 257, 512):
+        cx, cy = (float(v) for v in rng.uniform(-1.0, 1.0, 2))
+        nu = float(rng.uniform(0.01, 0.1))
+        dx = 1.0 / n
+        dt = 0.2 * dx * dx / nu
+        gx, gy = 0.5 * cx * dt / dx, 0.5 * cy * dt / dx
+        k = nu * dt / (dx * dx)
+        u = xgrid.Grid((n, n), float)
+        u.now[...] = rng.random((n, n)).astype(np.float32)
+        for _ in range(200):
+            convdiff(u, 1.0 - 4.0 * k, gx + k, k - gx, gy + k, k - gy)
+        out[f"u{n}"] = digests(u)
+    return out

@@ -35,3 +35,15 @@ def test_cavity_1025_5_steps_matches_reference_digests():
     native.Oracle("port").cavity(f, (1.0, 0.1, 1e-5, 2.0 / (n - 1), 2.0 / (n - 1)), 5)
     for k in "bpuv":
         assert _digests(f[k].levels) == ref[k], k
+
+
+def test_numpy_oracle_square_periodic_fp32_matches_reference_digests(tmp_path):
+    """The batched program's stencil on square periodic FP32 grids (64^2, 257^2,
+    512^2 for 200 steps): the numpy oracle runs the same program text as the
+    reference did."""
+    import sys
+    sys.path.insert(0, HERE)
+    from loader import load_cases
+    from oracle import xgrid_oracle
+    mod = load_cases(xgrid_oracle, str(tmp_path), "oracle", "full_cases.py")
+    assert mod.FULL["convdiff_square"]() == DIGESTS["convdiff_square"]
