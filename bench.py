@@ -211,7 +211,7 @@ class ClockSampler:
 def cpu_sample(n: int, steps: int) -> dict:
     """Run the reference C (or the C restatement) for ``steps`` steps; seconds."""
     from oracle import native
-    kind = "reference" if (native.ref_available() or os.path.isdir(native.REF)) else "port"
+    kind = "reference" if (native.ref_available() or native.ref_sources()) else "port"
     try:
         o = native.Oracle(kind, exact=False)
     except Exception:  # noqa: BLE001 - the reference sources are absent

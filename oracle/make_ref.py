@@ -1,6 +1,7 @@
 """Write the reference's own generated C for the benchmark programs.
 
-Needs the reference checkout (argv[1], default /root/reference).  For each of
+Needs the reference checkout: argv[1] or the environment variable
+``XGRID_REFERENCE``.  For each of
 the two benchmark programs in workloads.py (2-D diffusion, lid-driven cavity)
 it runs the reference's parser and C generator (xgrid/lang/generator.py) and
 writes the C source to oracle/_ref/<kernel>.c.  Those files are not versioned;
@@ -33,8 +34,14 @@ for name in {kernels!r}:
 """
 
 
-def generate(ref: str = "/root/reference") -> list:
-    if not os.path.isdir(os.path.join(ref, "xgrid")):
+def reference_checkout():
+    """Path of the reference checkout from ``XGRID_REFERENCE``, or None."""
+    ref = os.environ.get("XGRID_REFERENCE")
+    return ref if ref and os.path.isdir(os.path.join(ref, "xgrid")) else None
+
+
+def generate(ref: str) -> list:
+    if not ref or not os.path.isdir(os.path.join(ref, "xgrid")):
         raise FileNotFoundError(f"reference checkout not found at {ref}")
     os.makedirs(OUT, exist_ok=True)
     code = CHILD.format(ref=ref, root=ROOT, kernels=KERNELS, out=OUT)
@@ -44,5 +51,8 @@ def generate(ref: str = "/root/reference") -> list:
 
 
 if __name__ == "__main__":
-    for p in generate(*(sys.argv[1:2])):
+    checkout = sys.argv[1] if len(sys.argv) > 1 else reference_checkout()
+    if not checkout:
+        sys.exit("usage: make_ref.py <reference checkout> (or set XGRID_REFERENCE)")
+    for p in generate(checkout):
         print(p)

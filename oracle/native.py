@@ -26,7 +26,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD, "libxg_oracle.so")
-REFERENCE_CHECKOUT = "/root/reference"
 
 
 def _gcc(src: str, out: str, flags: list) -> None:
@@ -48,11 +47,13 @@ def build_oracle() -> str:
 
 def build_ref() -> list:
     """Compile the reference's generated C (generating it first when the
-    reference checkout is present and the sources are missing)."""
+    sources are missing and ``XGRID_REFERENCE`` names the reference checkout)."""
     sources = sorted(glob.glob(os.path.join(REF, "*.c")))
-    if not sources and os.path.isdir(os.path.join(REFERENCE_CHECKOUT, "xgrid")):
+    if not sources:
         from . import make_ref
-        sources = make_ref.generate(REFERENCE_CHECKOUT)
+        checkout = make_ref.reference_checkout()
+        if checkout:
+            sources = make_ref.generate(checkout)
     built = []
     for src in sources:
         base = src[:-2]
@@ -66,6 +67,11 @@ def build_ref() -> list:
 def build_all() -> None:
     build_oracle()
     build_ref()
+
+
+def ref_sources() -> list:
+    """The reference's generated C sources written by ``make_ref.py``."""
+    return sorted(glob.glob(os.path.join(REF, "*.c")))
 
 
 def ref_available() -> bool:
@@ -100,8 +106,10 @@ def _ip(a: np.ndarray):
 class Field:
     """Two time levels and a mask, rotated like the reference's Grid."""
 
-    def __init__(self, level0: np.ndarray, mask: np.ndarray) -> None:
-        self.levels = [np.ascontiguousarray(level0, dtype=np.float64).copy(), np.zeros_like(level0, dtype=np.float64)]
+    def __init__(self, level0: np.ndarray, mask: np.ndarray, level1=None) -> None:
+        self.levels = [np.ascontiguousarray(level0, dtype=np.float64).copy(),
+                       np.zeros_like(level0, dtype=np.float64) if level1 is None
+                       else np.ascontiguousarray(level1, dtype=np.float64).copy()]
         self.mask = np.ascontiguousarray(mask, dtype=np.int32)
         self._ptrs = None
 
@@ -172,10 +180,15 @@ class Oracle:
                                        f["v"].ref_struct(), g)
 
 
-def cavity_fields(n: int) -> dict:
+def cavity_fields(n: int, seed=None) -> dict:
+    """Cavity grids with the benchmark's masks: zero fields, or both levels from
+    ``workloads.cavity_state(n, seed)``."""
     import workloads
     masks = workloads.cavity_masks(n)
-    return {k: Field(np.zeros((n, n)), masks[k]) for k in "bpuv"}
+    if seed is None:
+        return {k: Field(np.zeros((n, n)), masks[k]) for k in "bpuv"}
+    state = workloads.cavity_state(n, seed)
+    return {k: Field(state[k][0], masks[k], state[k][1]) for k in "bpuv"}
 
 
 def diffusion_field(n: int = 512, seed: int = 0) -> tuple:

@@ -1,7 +1,8 @@
 """Record the digests of ``full_cases.py`` by running the reference implementation.
 
-Run in a checkout that has the reference package available (path in argv[1],
-default /root/reference).  Each case runs in its own process with the
+Run where the reference package is available: its checkout path comes from
+argv[1] or the environment variable ``XGRID_REFERENCE``; further arguments
+name the cases to record (default: all; the others keep their digests).  Each case runs in its own process with the
 reference's ``xgrid`` (its C backend compiled by gcc, OpenMP on); the SHA-256 of
 every time level of every grid goes to ``full_digests.json`` beside this script.
 """
@@ -26,11 +27,14 @@ print(json.dumps(mod.FULL[{case!r}]()))
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XGRID_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_digests.py <reference checkout> [case ...] (or set XGRID_REFERENCE)")
     sys.path.insert(0, HERE)
     from loader import load_cases
-    names = list(load_cases(None, "", "names", "full_cases.py").FULL)
-    out = {}
+    names = sys.argv[2:] or list(load_cases(None, "", "names", "full_cases.py").FULL)
+    path = os.path.join(HERE, "full_digests.json")
+    out = json.load(open(path)) if os.path.exists(path) else {}
     for case in names:
         with tempfile.TemporaryDirectory() as tmp:
             code = CHILD.format(ref=ref, here=HERE, case=case)
@@ -42,7 +46,7 @@ def main() -> None:
             continue
         out[case] = json.loads(proc.stdout.strip().splitlines()[-1])
         print(case, "ok")
-    with open(os.path.join(HERE, "full_digests.json"), "w") as f:
+    with open(path, "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
 
 

@@ -1,7 +1,8 @@
 """Record golden vectors by running the reference implementation.
 
-Run in a checkout that has the reference package available (path in argv[1],
-default /root/reference).  Each case of ``cases.py`` runs in its own process
+Run where the reference package is available: its checkout path comes from
+argv[1] or the environment variable ``XGRID_REFERENCE``; further arguments name
+the cases to record (default: all).  Each case of ``cases.py`` runs in its own process
 with the reference's ``xgrid`` (its C backend compiled by gcc, OpenMP on) and
 its outputs are written to ``<case>.npz`` beside this script.  The cases only
 use inputs the reference handles correctly (see ``cases.py``).
@@ -28,13 +29,17 @@ np.savez_compressed({dst!r}, **out)
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("XGRID_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout> (or set XGRID_REFERENCE)")
     sys.path.insert(0, HERE)
     names = [l.split("def ", 1)[1].split("(")[0] for l, prev in
              zip(open(os.path.join(HERE, "cases.py")).read().splitlines()[1:],
                  open(os.path.join(HERE, "cases.py")).read().splitlines())
              if prev.strip() == "@case"]
-    meta = {}
+    names = sys.argv[2:] or names
+    index = os.path.join(HERE, "golden_index.json")
+    meta = json.load(open(index)) if os.path.exists(index) else {}
     for case in names:
         dst = os.path.join(HERE, f"{case}.npz")
         with tempfile.TemporaryDirectory() as tmp:
@@ -46,7 +51,7 @@ def main() -> None:
         print(case, status)
         if proc.returncode != 0:
             print(proc.stderr[-2000:])
-    with open(os.path.join(HERE, "golden_index.json"), "w") as f:
+    with open(index, "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
 
 

@@ -62,6 +62,10 @@ def implicit_after_write(p: g2, q: g2) -> None:
     p[0, 0] = 0.5 * (p[1, 0][0] + p[-1, 0][0])
 
 
+def store_at_a_time_offset(q: g2) -> None:
+    q[0, 0][-1] = 0.5 * (q[0, 1][0] + q[0, -1][0])
+
+
 def test_offset_read_of_a_fresh_write_splits():
     assert _shape(_groups(offset_read_of_fresh_write)) == [["main"], ["main"]]
 
@@ -93,6 +97,14 @@ def test_main_after_boundary_opens_a_group():
 def test_implicit_sweep_after_a_write_of_its_input_splits():
     shape = _shape(_groups(implicit_after_write))
     assert shape == [["main"], ["main*"]]
+
+
+def test_store_at_a_time_offset_is_rejected_like_the_reference():
+    """``g[o][t] = ...`` is a load in the target position: the reference dies with
+    this message (xgrid/lang/generator.py:62-65), so every sweep writes level 0."""
+    import pytest
+    with pytest.raises(Exception, match="Unable to perform load operation to grid 'q' without stencil context"):
+        _groups(store_at_a_time_offset)
 
 
 def test_no_fusion_gives_one_launch_per_sweep():

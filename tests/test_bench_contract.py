@@ -7,15 +7,10 @@ import os
 import subprocess
 import sys
 
-import pytest
-
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_reference_arm_prints_one_contract_line():
-    from oracle import native
-    if not native.ref_available() and not os.path.isdir(native.REFERENCE_CHECKOUT):
-        pytest.skip("reference generated C not present")
     proc = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "2", "--warmup", "1",
                            "--n", "129", "--cpu-seconds", "1"], cwd=ROOT, capture_output=True, text=True,
                           timeout=600)

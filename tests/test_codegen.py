@@ -159,3 +159,35 @@ def test_argument_names_do_not_collide_with_generated_names(tmp_path):
     Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)
     m = CudaGenerator(Operator(returning, "kernel", "returning"), get_config()).generate()
     Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)
+
+
+def noalloc_in_place(q: xgrid.grid[float, 2], r: xgrid.grid[float, 2]) -> None:
+    q[0, 0] = 0.25 * (q[1, 0][0] + q[-1, 0][0] + q[0, 1][0] + q[0, -1][0])
+    r[0, 0] = 0.5 * (r[0, 1][0] + q[0, 0][0])
+
+
+def noalloc_explicit(u: xgrid.grid[float, 2], c: float) -> None:
+    u[0, 0] = u[0, 0] + c * (u[0, 1] - u[0, 0])
+
+
+def noalloc_scalar(a: int, b: int) -> int:
+    return a * b + 1
+
+
+@pytest.mark.skipif(shutil.which("nvcc") is None, reason="nvcc not available")
+def test_noalloc_entry_is_exported_by_every_kind_of_kernel(tmp_path):
+    """``noalloc=True`` always exports ``xg_kernel_<name>_noalloc``: with a scratch
+    pool and the level-permutation undo when the kernel has in-place sweeps, as a
+    plain table-build guard otherwise (also for kernels without grids)."""
+    from xgrid_gb300.compiler import Compiler
+    xgrid.init(precision="double", cacheroot="/tmp/xgcg", opt_level=3)
+    for fn, pool in ((noalloc_in_place, True), (noalloc_explicit, False), (noalloc_scalar, False)):
+        op = Operator(fn, "kernel", fn.__name__)
+        op.noalloc = True
+        m = CudaGenerator(op, get_config()).generate()
+        assert f"xg_kernel_{fn.__name__}_noalloc(" in m.source
+        assert (f"xg_noalloc_pool_{fn.__name__}[" in m.source) == pool
+        assert "cudaMalloc" not in m.source.split(f"xg_kernel_{fn.__name__}_noalloc(")[1]
+        lib = Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)
+        out = __import__("subprocess").run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True).stdout
+        assert f"xg_kernel_{fn.__name__}_noalloc" in out

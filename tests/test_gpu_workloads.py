@@ -40,6 +40,25 @@ def test_cavity_bitexact(cacheroot, n, steps):
             assert _bits_equal(grids[k].read(lv), f[k].levels[lv]), f"{k} level {lv}"
 
 
+@pytest.mark.parametrize("n,dt,steps,seed", [(1025, 5e-6, 20, 7), (4097, 5e-7, 3, 8)])
+def test_cavity_seeded_every_cell_bitexact(cacheroot, n, dt, steps, seed):
+    """Seeded random b, p, u, v in every cell of both levels (no cell compares zero
+    with zero): 1025^2 at the benchmark's dt for 20 steps, 4097^2 for 3 steps.
+    The C oracle reproduces the reference's own digests of these runs
+    (tests/test_oracle_full.py), so this is GPU = reference, every level of every grid."""
+    xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3)
+    grids, cfg = workloads.cavity_setup(n, dt, seed=seed)
+    for _ in range(steps):
+        workloads.cavity_kernel(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+    f = native.cavity_fields(n, seed)
+    native.Oracle("port").cavity(f, (cfg.rho, cfg.nu, cfg.dt, cfg.dx, cfg.dy), steps)
+    for k in "bpuv":
+        for lv in range(2):
+            got = grids[k].read(lv)
+            assert np.isfinite(got).all(), f"{k} level {lv}"
+            assert _bits_equal(got, f[k].levels[lv]), f"{k} level {lv}"
+
+
 def test_cavity_unfused_and_eager_match(cacheroot):
     """Every launch strategy computes the same bits: fused groups + graphs,
     one launch per sweep, eager calls."""

@@ -28,8 +28,8 @@ def test_c_oracle_diffusion_matches_golden():
     assert np.stack(field.levels).tobytes() == g.tobytes()
 
 
-@pytest.mark.skipif(not (native.ref_available() or os.path.isdir(native.REFERENCE_CHECKOUT)),
-                    reason="reference checkout and generated C not present")
+@pytest.mark.skipif(not (native.ref_available() or native.ref_sources()),
+                    reason="the reference's generated C is not present (oracle/make_ref.py writes it)")
 @pytest.mark.parametrize("n,steps", [(65, 4), (129, 2)])
 def test_c_oracle_matches_reference_generated_c(n, steps):
     out = []

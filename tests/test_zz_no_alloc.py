@@ -42,26 +42,37 @@ def _grids(n: int, seed: int):
     return p, f
 
 
-def _call_noalloc(p, f, iters: int, h2: float) -> int:
-    """Call the no-alloc entry point directly through the C ABI."""
-    nk = relax.native
-    fn = nk.lib.entry("xg_kernel_relax_noalloc")
+def _call_noalloc(p, f, iters: int, h2: float, kern=None) -> int:
+    """Call the no-alloc entry point of ``kern`` (default ``relax``) on (p, f)."""
+    return _call_grids(kern or relax, [p, f], [iters, h2])
+
+
+def _call_grids(kern, grids, values) -> int:
+    """Call ``xg_kernel_<name>_noalloc`` directly through the C ABI, checking that
+    the caller's level pointers stay put and that free device memory does not
+    change across the call."""
+    import torch
+    nk = kern.native
+    fn = nk.lib.entry(f"xg_kernel_{nk.module.name}_noalloc")
     fn.restype = ctypes.c_int
     fn.argtypes = [ctypes.POINTER(runtime.XGGrid), ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
                    ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
-    for g in (p, f):
+    for g in grids:
         g._op_invoke(nk.depth, True)
         g._sync_device(False)
     device.stream().synchronize()
-    arr = (runtime.XGGrid * 2)(p.serialize(), f.serialize())
-    before = [arr[0].level[0], arr[1].level[0]]
-    packed = nk.pack([iters, h2])
-    rc = fn(arr, 2, ctypes.cast(ctypes.byref(packed), ctypes.c_void_p), ctypes.sizeof(packed), None, 0,
+    arr = (runtime.XGGrid * len(grids))(*[g.serialize() for g in grids])
+    before = [[st.level[i] for i in range(st.levels)] for st in arr]
+    packed = nk.pack(values)
+    free0 = torch.cuda.mem_get_info()[0]
+    rc = fn(arr, len(grids), ctypes.cast(ctypes.byref(packed), ctypes.c_void_p), ctypes.sizeof(packed), None, 0,
             device.stream_handle())
     device.stream().synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0, "the no-alloc call changed free device memory"
     if rc == 0:
-        assert [arr[0].level[0], arr[1].level[0]] == before, "the caller's level pointers must not change"
-        for g, st in zip((p, f), arr):
+        assert [[st.level[i] for i in range(st.levels)] for st in arr] == before, \
+            "the caller's level pointers must not change"
+        for g, st in zip(grids, arr):
             g._adopt(st)
     return rc
 
@@ -108,3 +119,25 @@ def test_noalloc_rejects_grids_beyond_the_pool(tmp_path):
     rc = _call_noalloc(p, f, 1, 0.01)
     assert rc != 0
     assert "more than the" in runtime.last_error()
+
+
+@pytest.mark.parametrize("mode", ["persistent", "mixed"])
+def test_noalloc_persistent_and_mixed_loops_match_regular_entry(tmp_path, mode):
+    """The persistent loop launch and the mixed-precision loop: warmed up by one
+    regular call with the same arguments, the no-alloc call gives the regular
+    entry's bits (the mixed loop uses the grid's work area, which the caller
+    provides like the levels)."""
+    kw = {"persistent": True} if mode == "persistent" else {"mixed": "fp32"}
+    xgrid.init(precision="double", cacheroot=_cache(tmp_path), opt_level=3, **kw)
+    kern = xgrid.kernel(noalloc=True)(relax.func)
+    n = 120
+    pa, fa = _grids(n, 21)
+    pb, fb = _grids(n, 21)
+    p0, f0 = pa.read(0), fa.read(0)
+    kern(pb, fb, 9, 0.01)
+    pb.now[...] = p0
+    fb.now[...] = f0
+    for iters in (9, 9):
+        kern(pa, fa, iters, 0.01)
+        assert _call_noalloc(pb, fb, iters, 0.01, kern) == 0, runtime.last_error()
+        assert pa.read(0).tobytes() == pb.read(0).tobytes()

@@ -124,11 +124,25 @@ def cavity_masks(n: int) -> dict:
     return m
 
 
-def cavity_setup(n: int = 1025, dt: float = 1e-5):
-    """Zero u, v, p, b on [0,2]^2 with n x n points, rho=1, nu=0.1."""
+def cavity_state(n: int, seed: int) -> dict:
+    """Seeded initial levels of the cavity grids: U[0, 1) for level 0 then level 1
+    of b, p, u and v, in that order, from one generator (every cell live, the
+    boundary cells of b included, which the program never writes)."""
+    rng = np.random.default_rng(seed)
+    return {k: [rng.random((n, n)) for _ in range(2)] for k in "bpuv"}
+
+
+def cavity_setup(n: int = 1025, dt: float = 1e-5, seed=None):
+    """u, v, p, b on [0,2]^2 with n x n points, rho=1, nu=0.1: zero fields, or
+    both time levels from ``cavity_state(n, seed)``."""
     grids = {k: xgrid.Grid((n, n), float) for k in "bpuv"}
     for k, mask in cavity_masks(n).items():
         grids[k].boundary[...] = mask
+    if seed is not None:
+        for k, levels in cavity_state(n, seed).items():
+            grids[k]._extend_time(2)
+            for lv, x in enumerate(levels):
+                grids[k]._data[lv][...] = x
     cfg = Config(1.0, 0.1, dt, 2.0 / (n - 1), 2.0 / (n - 1))
     return grids, cfg
 

@@ -94,6 +94,11 @@ def classify(stmt: ir.Assignment, slots: dict, logger: Logger) -> Sweep:
     """Tag one grid assignment (xgrid/lang/generator.py:57-76)."""
     target = stmt.terminal
     assert isinstance(target, ir.Stencil)
+    if target.context != "store":
+        # g[o][t] = ... : the time subscript makes the grid access a load
+        # (xgrid/lang/parser.py:509-518), which the reference rejects as a target
+        # (xgrid/lang/generator.py:62-65); every sweep writes level 0
+        logger.dead(f"Unable to perform load operation to grid '{target.variable.name}' without stencil context")
     sweep = Sweep(stmt, slots[target.variable.name], target.boundary_mask, False,
                   abs(target.time_offset), pad3(target.space_offset))
     for node in ir.walk(stmt.value):

@@ -568,7 +568,7 @@ class CudaGenerator:
         src.append("  return e;")
         src.append("}")
         implicit = sorted({s.slot for s in self.sweeps if s.implicit})
-        if getattr(self.op, "noalloc", False) and grid_args and implicit:
+        if getattr(self.op, "noalloc", False):
             src.extend(self.noalloc_entry(name, entry, grid_args, implicit))
         return Module("\n".join(src) + "\n", name, entry, self.depth + 1, grid_args, value_args, order, rtype,
                       implicit, dict(self.mixed_slots), batch_host is not None, self.group_counter[0], device_only,
@@ -578,8 +578,23 @@ class CudaGenerator:
         """``<entry>_noalloc``: same computation as ``<entry>``, for callers that
         cannot allocate device memory.  The scratch level of every grid that an
         in-place (two-phase) sweep needs is carved out of one file-scope device
-        array; after the call, a level left in that array is copied back into
-        the caller's buffer, so the caller's level pointers never change."""
+        array.  The call exchanges level and scratch buffers as the regular entry
+        does, which leaves each such grid's levels permuted among the caller's
+        buffers and the array; afterwards device copies put every level's result
+        back into the caller's buffer of that level (the buffer left holding no
+        level serves as the spare that breaks cycles), so the caller's level
+        pointers never change.  Kernels without in-place sweeps get a wrapper
+        that only forbids table builds (they need no scratch)."""
+        head = [f'extern "C" int {entry}_noalloc(xg_grid* G, int ngrids, const void* args, size_t nargs, void* ret, '
+                f'size_t nret, void* stream) {{']
+        if not implicit:
+            return head + [
+                "  // no in-place sweep: no scratch; a missing mask table is an error, not an allocation",
+                "  xg_internal_noalloc_scope(1);",
+                f"  const int rc = {entry}(G, ngrids, args, nargs, ret, nret, stream);",
+                "  xg_internal_noalloc_scope(0);",
+                "  return rc;",
+                "}"]
         elems = ", ".join(f"sizeof({c_type(grid_args[s][1].element)})" for s in implicit)
         slots = ", ".join(str(s) for s in implicit)
         k = len(implicit)
@@ -591,8 +606,7 @@ class CudaGenerator:
             "#define XG_NOALLOC_MAX_DEVICES 64",
             f"static __device__ __align__(256) unsigned char {pool}[XG_NOALLOC_POOL_BYTES];",
             f"static void* {pool}_addr[XG_NOALLOC_MAX_DEVICES];",
-            f'extern "C" int {entry}_noalloc(xg_grid* G, int ngrids, const void* args, size_t nargs, void* ret, '
-            f'size_t nret, void* stream) {{',
+        ] + head + [
             "  cudaStream_t s = (cudaStream_t)stream;",
             f"  if (ngrids != {len(grid_args)}) XG_FAIL(\"{name}_noalloc: expected {len(grid_args)} grids, got %d\", "
             f"ngrids);",
@@ -623,14 +637,36 @@ class CudaGenerator:
             f"  int rc = {entry}(L, ngrids, args, nargs, ret, nret, stream);",
             "  xg_internal_noalloc_scope(0);",
             "  if (rc != 0) return rc;",
-            "  // a level that ended in the pool (odd number of exchanges) goes back to the caller's buffer",
+            "  // undo the level permutation: the level whose caller buffer is the spare moves",
+            "  // there (its old buffer becomes the spare); when none does, the rest are cycles",
+            "  // among the caller's buffers and one of them moves to the spare (the pool) first",
             f"  for (int i = 0; i < {k}; ++i) {{",
             "    const int g = slots[i];",
-            "    for (int lv = 0; lv < L[g].levels && lv < XG_MAX_LEVELS; ++lv) {",
-            "      unsigned char* q = (unsigned char*)L[g].level[lv];",
-            "      if (q >= base && q < base + XG_NOALLOC_POOL_BYTES)",
-            "        XG_CUDA(cudaMemcpyAsync(G[g].level[lv], q, bytes[i], cudaMemcpyDeviceToDevice, s));",
+            "    const int nl = L[g].levels < XG_MAX_LEVELS ? L[g].levels : XG_MAX_LEVELS;",
+            "    void* spare = L[g].scratch;",
+            "    for (int round = 0; round < 2 * XG_MAX_LEVELS + 2; ++round) {",
+            "      int pending = -1, moved = 0;",
+            "      for (int lv = 0; lv < nl; ++lv) {",
+            "        if (L[g].level[lv] == G[g].level[lv]) continue;",
+            "        pending = lv;",
+            "        if (G[g].level[lv] == spare) {",
+            "          XG_CUDA(cudaMemcpyAsync(G[g].level[lv], L[g].level[lv], bytes[i], cudaMemcpyDeviceToDevice, s));",
+            "          spare = L[g].level[lv];",
+            "          L[g].level[lv] = G[g].level[lv];",
+            "          moved = 1;",
+            "        }",
+            "      }",
+            "      if (pending < 0) break;",
+            "      if (!moved) {",
+            "        XG_CUDA(cudaMemcpyAsync(spare, L[g].level[pending], bytes[i], cudaMemcpyDeviceToDevice, s));",
+            "        void* t_ = L[g].level[pending];",
+            "        L[g].level[pending] = spare;",
+            "        spare = t_;",
+            "      }",
             "    }",
+            "    for (int lv = 0; lv < nl; ++lv)",
+            "      if (L[g].level[lv] != G[g].level[lv])",
+            f"        XG_FAIL(\"{name}_noalloc: internal error, level %d of grid %d not restored\", lv, g);",
             "  }",
             "  return 0;",
             "}",

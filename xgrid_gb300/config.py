@@ -37,6 +37,11 @@ Backend options (new keywords, all optional):
   one launch per iteration; same arithmetic, same bits.  Off by default: on a
   GB300 the grid barrier of ~600 CTAs costs more than a launch boundary inside
   a CUDA graph (cavity 1025^2: 1.12x the step time).
+* ``fail_waits``: for testing only.  Compile modules whose give-up waits cannot
+  succeed (the grid barrier of a persistent loop polls once; a TMA staging
+  barrier expects more bytes than its copies deliver), so that those waits run
+  out: the kernel sets its error word and returns, after draining its copies.
+  Results of such modules are invalid by construction.
 * ``graph``: capture each distinct kernel call into a CUDA graph and replay it.
 * ``fuse``: fuse consecutive sweeps into one launch where the masks allow it.
 * ``divisor``: precompute loop-invariant divisors on the host and divide with a
@@ -81,6 +86,7 @@ class Configuration:
     mixed_rows: int = 16
     int_adds: int = 0
     persistent: bool = False
+    fail_waits: bool = False
 
     def __repr__(self) -> str:
         return repr(dataclasses.asdict(self))
@@ -94,6 +100,8 @@ class Configuration:
         flags = [f"-O{self.opt_level}"]
         if self.exact:
             flags += ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]
+        if self.fail_waits:
+            flags.append("-DXG_FAIL_WAITS")
         return flags
 
 
@@ -111,7 +119,8 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
          opt_level: Literal[0, 1, 2, 3] = 2, precision: Literal["float", "double"] = "float",
          exact: bool = True, mixed: Optional[str] = None, graph: bool = True,
          fuse: bool = True, divisor: bool = True, mixed_every: int = 0, autotune: bool = True,
-         mixed_temporal: int = 4, mixed_rows: int = 16, int_adds: int = 0, persistent: bool = False) -> None:
+         mixed_temporal: int = 4, mixed_rows: int = 16, int_adds: int = 0, persistent: bool = False,
+         fail_waits: bool = False) -> None:
     """Set the global configuration (same keywords as the reference plus GPU options)."""
     global _config
     if sys.version_info < (3, 10):
@@ -132,5 +141,6 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
         logger.dead(f"Invalid mixed_rows {mixed_rows}, expected one of {MIXED_ROWS}")
     _config = Configuration(parallel, list(cc), cacheroot, comment, overstep, opt_level,
                             precision, exact, mixed, graph, fuse, divisor, int(mixed_every), bool(autotune),
-                            int(mixed_temporal), int(mixed_rows), int(int_adds), bool(persistent))
+                            int(mixed_temporal), int(mixed_rows), int(int_adds), bool(persistent),
+                            bool(fail_waits))
     logger.info(f"initialized with configuration: {_config}")

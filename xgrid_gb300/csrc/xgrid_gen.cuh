@@ -345,10 +345,36 @@ __device__ __forceinline__ void xg_tma_load_2d(void* dst, const CUtensorMap* map
       : "memory");
 }
 
-// Poll phase `parity` of an mbarrier at most `limit` times; false when it did not complete.
-#define XG_WAIT_LIMIT (1u << 22)
-__device__ __forceinline__ bool xg_mbar_wait(uint64_t* bar, unsigned parity, unsigned limit) {
-  for (unsigned i = 0; i < limit; ++i) {
+// Bounded waits.  Every device-side wait gives up after XG_WAIT_NS nanoseconds of
+// the global timer (about a second; the copies and barriers it waits for take
+// microseconds).  The waits whose give-up path reports an error and leaves (the
+// first wait for a TMA staging copy, the grid barrier of a persistent loop) use
+// XG_GIVEUP_NS, the same by default.  A module compiled with XG_FAIL_WAITS makes
+// those waits unable to succeed, to test the give-up paths: the grid barrier polls
+// once, and a TMA staging barrier expects 16 bytes more than its copies deliver
+// (the copies themselves still land, and the CTA drains them before it leaves).
+#ifndef XG_WAIT_NS
+#define XG_WAIT_NS 1000000000ull
+#endif
+#ifdef XG_FAIL_WAITS
+#define XG_GIVEUP_NS 0ull
+#define XG_TMA_TX_EXTRA 16u
+#else
+#define XG_GIVEUP_NS XG_WAIT_NS
+#define XG_TMA_TX_EXTRA 0u
+#endif
+#define XG_WAIT_POLLS_MAX (1u << 30)  // a second bound that does not depend on the timer
+
+__device__ __forceinline__ uint64_t xg_now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for phase `parity` of an mbarrier for at most `limit_ns`; false when it did not complete.
+__device__ __forceinline__ bool xg_mbar_wait(uint64_t* bar, unsigned parity, uint64_t limit_ns) {
+  const uint64_t t0 = xg_now_ns();
+  for (unsigned i = 0; i < XG_WAIT_POLLS_MAX; ++i) {
     unsigned done = 0;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -356,6 +382,7 @@ __device__ __forceinline__ bool xg_mbar_wait(uint64_t* bar, unsigned parity, uns
         : "r"(xg_smem_addr(bar)), "r"(parity)
         : "memory");
     if (done) return true;
+    if (xg_now_ns() - t0 >= limit_ns) return false;
   }
   return false;
 }
@@ -384,7 +411,7 @@ __device__ __forceinline__ xg_tile xg_tile_at(int64_t t, int64_t Z, int64_t Y, i
 // sync[0] counts arrivals (zero at launch); barrier `gen` is complete when it
 // reaches gen * nblocks.  Thread 0 of each CTA arrives with a release and polls
 // with acquires, so the writes of every CTA before the barrier are visible to
-// every CTA after it.  The poll is bounded: after XG_WAIT_LIMIT polls it sets
+// every CTA after it.  The poll is bounded: after XG_GIVEUP_NS nanoseconds it sets
 // the error word sync[1] and the CTA leaves (false).
 __device__ __forceinline__ bool xg_grid_sync(unsigned* sync, unsigned nblocks, unsigned gen) {
   __shared__ int ok_;
@@ -394,13 +421,15 @@ __device__ __forceinline__ bool xg_grid_sync(unsigned* sync, unsigned nblocks, u
     __threadfence();
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(sync), "r"(1u) : "memory");
     int ok = 0;
-    for (unsigned i = 0; i < XG_WAIT_LIMIT; ++i) {
+    const uint64_t t0 = xg_now_ns();
+    for (unsigned i = 0; i < XG_WAIT_POLLS_MAX; ++i) {
       unsigned v;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(sync) : "memory");
       if ((int)(v - target) >= 0) {
         ok = 1;
         break;
       }
+      if (xg_now_ns() - t0 >= XG_GIVEUP_NS) break;
     }
     if (!ok) atomicExch((int*)(sync + 1), 1);
     __threadfence();

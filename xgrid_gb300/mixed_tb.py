@@ -137,15 +137,16 @@ class TemporalDefect:
              "  __syncthreads();",
              "  if (tid == 0) {",
              "    const unsigned rb = (p.first || !scaled) ? 4u : (unsigned)sizeof(Dt);",
-             "    xg_mbar_expect_tx(&xg_bar, (unsigned)(BY * BX) * (rb + (p.first ? 0u : (unsigned)sizeof(Dt))));",
+             "    xg_mbar_expect_tx(&xg_bar, (unsigned)(BY * BX) * (rb + (p.first ? 0u : (unsigned)sizeof(Dt))) + "
+             "XG_TMA_TX_EXTRA);",
              "    xg_tma_load_2d(sB, &p.mr, bx, by, &xg_bar);",
              "    if (!p.first) xg_tma_load_2d(sA, &p.md, bx, by, &xg_bar);",
              "  }",
-             "  const bool landed = xg_mbar_wait(&xg_bar, 0, XG_WAIT_LIMIT);",
+             "  const bool landed = xg_mbar_wait(&xg_bar, 0, XG_GIVEUP_NS);",
              "  if (__syncthreads_or(!landed)) {  // the copy did not complete: report, let it drain, stop",
              "    if (tid == 0) {",
              "      atomicExch(p.err, 1);",
-             "      xg_mbar_wait(&xg_bar, 0, XG_WAIT_LIMIT);",
+             "      xg_mbar_wait(&xg_bar, 0, XG_WAIT_NS);",
              "    }",
              "    return;",
              "  }",

@@ -78,6 +78,23 @@ class NativeKernel:
             self.logger.dead("reading the persistent-loop error word failed")
         return rc
 
+    def staging_error(self, grid, clear: bool = False) -> int:
+        """1 when a TMA staging copy of a mixed-precision loop on ``grid`` did not
+        complete in time (the results of that call are invalid), else 0; ``clear``
+        resets the word.  Synchronises with the device."""
+        aux = getattr(grid, "_aux", None)
+        if aux is None:
+            return 0
+        off = mixed.aux_error_offset(grid.shape)
+        device.stream().synchronize()
+        word = aux[off:off + 4]
+        err = int(np.frombuffer(word.cpu().numpy().tobytes(), dtype=np.int32)[0])
+        if clear and err:
+            with device.torch().cuda.stream(device.stream()):
+                word.zero_()
+            device.stream().synchronize()
+        return 1 if err else 0
+
     # ---------------------------------------------------------------- tuning
     def set_tiling(self, group: int, tiling: tuple) -> None:
         """(tz, ty, tx, block.x, block.y, block.z) for one launch group."""
