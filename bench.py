@@ -14,14 +14,22 @@ update per cell per full-grid sweep (54 per step; boundary passes excluded).
   reads ``u.now``, ``v.now``, ``p.now`` back (device→host) and the next call
   uploads them again (host→device, pinned), wall clock around the loop.
 * ``roofline``: the dominant kernel (the fused Jacobi + boundary launch), its
-  algorithmic bytes per launch over its mean duration from CUDA events recorded
-  around every launch during a profiled (non-graph) pass of the same steps.
+  algorithmic bytes per launch over its mean duration inside the CUDA graphs the
+  timed region replays (event-record nodes around every launch, L2 flushed
+  between steps as in the timed region).
 * ``cpu_baseline``: the reference's own generated C (compiled from
   ``oracle/_ref``) on all host cores for a bounded number of steps.
+
+The same line carries one section per further configuration, each with its own
+``roofline``, ``cpu_baseline`` and ``e2e``: ``diffusion`` (2-D FTCS 512^2 FP64,
+500 steps), ``mixed`` (cavity 4097^2, FP32 / FP16 / BF16 defect correction vs
+plain FP64), ``batched`` (256 periodic FP32 problems of uneven size, 1000
+steps) and ``adjoint`` (3-D 256^3 FP32 rollout and gradient).
 
 ``--impl reference`` times that reference C path alone on the host cores.
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -67,6 +75,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile shapes of the headline kernel")
     ap.add_argument("--cpu-sample", type=int, default=0, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-workload", default="cavity", help=argparse.SUPPRESS)
     ap.add_argument("--mixed-n", type=int, default=4097)
     ap.add_argument("--mixed-steps", type=int, default=500)
     ap.add_argument("--no-mixed", action="store_true")
@@ -76,6 +85,10 @@ def parse_args():
     ap.add_argument("--adjoint-n", type=int, default=256)
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-diffusion", action="store_true")
+    ap.add_argument("--persistent", type=int, default=0,
+                    help="headline: run the pressure loop as one persistent launch per step (1) or one launch "
+                         "per iteration (0)")
     ap.add_argument("--mixed", default=None, choices=[None, "fp32", "fp16", "bf16"],
                     help="kernels mode: precision lowering of the pressure loop")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "batch", "adjoint"],
@@ -123,7 +136,7 @@ def kernels_only(args) -> None:
         print(json.dumps({"mode": "kernels", "workload": "adjoint", "n": args.n, "calls": args.warmup + 1}))
         return
     xgrid.init(precision="double", cacheroot=JIT_CACHE,
-               opt_level=3, mixed=args.mixed, mixed_temporal=args.mixed_temporal)
+               opt_level=3, mixed=args.mixed, mixed_temporal=args.mixed_temporal, persistent=bool(args.persistent))
     grids, cfg = workloads.cavity_setup(args.n, stable_dt(args.n))
     for _ in range(args.warmup + args.steps):
         workloads.cavity_kernel(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
@@ -208,38 +221,105 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU side
-def cpu_sample(n: int, steps: int) -> dict:
-    """Run the reference C (or the C restatement) for ``steps`` steps; seconds."""
+def cpu_sample(workload: str, n: int, steps: int) -> dict:
+    """Time ``steps`` steps of a workload on the host cores (run in a child process
+    whose OpenMP / torch thread count is the core count): the reference's own
+    generated C (``oracle/_ref``) where it exists, else the C restatement, and
+    torch CPU autograd for the 3-D adjoint (the reference mis-indexes 3-D grids).
+    Returns seconds and what ran."""
+    import numpy as np
+
     from oracle import native
+    if workload == "adjoint":
+        import torch
+        torch.set_num_threads(os.cpu_count() or 1)
+        u0, kap, tgt, dt = workloads_mod().adjoint_setup(n, 2)
+        u0, kap, tgt = (torch.tensor(x) for x in (u0, kap, tgt))
+        torch_autograd_run(u0, kap, tgt, dt, 1)  # warm-up
+        t0 = time.perf_counter()
+        torch_autograd_run(u0, kap, tgt, dt, steps)
+        return {"kind": "torch-cpu-autograd", "seconds": time.perf_counter() - t0, "steps": steps,
+                "threads": torch.get_num_threads()}
+    if workload == "convdiff":
+        # equal-cell squares of the batched problems (the reference strides
+        # non-square grids by the wrong extent): timing only, one call per problem
+        run = native.convdiff_reference()
+        fields = []
+        for u0, coeffs in workloads_mod().batch_params(256, seed=1):
+            side = int(round(float(np.sqrt(u0.size))))
+            fields.append((native.Field32(np.resize(u0, (side, side))), tuple(np.float32(c) for c in coeffs)))
+        for f, c in fields:
+            run(f, c, 1)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            for f, c in fields:
+                run(f, c, 1)
+        return {"kind": "reference", "seconds": time.perf_counter() - t0, "steps": steps,
+                "cells": sum(int(f.levels[0].size) for f, _ in fields)}
     kind = "reference" if (native.ref_available() or native.ref_sources()) else "port"
     try:
         o = native.Oracle(kind, exact=False)
     except Exception:  # noqa: BLE001 - the reference sources are absent
         kind = "port"
         o = native.Oracle("port")
+    if workload == "diffusion":
+        field, c = native.diffusion_field(n, seed=0)
+        o.diffusion(field, c, 1)
+        t0 = time.perf_counter()
+        o.diffusion(field, c, steps)
+        return {"kind": kind, "seconds": time.perf_counter() - t0, "steps": steps}
     f = native.cavity_fields(n)
     cfg = (1.0, 0.1, stable_dt(n), 2.0 / (n - 1), 2.0 / (n - 1))
     o.cavity(f, cfg, 1)  # warm-up (page faults, thread team)
     t0 = time.perf_counter()
     o.cavity(f, cfg, steps)
-    dt = time.perf_counter() - t0
-    return {"kind": kind, "seconds": dt, "steps": steps}
+    return {"kind": kind, "seconds": time.perf_counter() - t0, "steps": steps}
 
 
-def run_cpu(n: int, steps: int) -> dict:
+def workloads_mod():
+    import workloads
+    return workloads
+
+
+def torch_autograd_run(u0, kap, tgt, dt: float, steps: int) -> float:
+    """Forward rollout and gradient of the 3-D variable-coefficient diffusion
+    through plain torch tensor ops (periodic shifts), on the tensors' device."""
+    import torch
+    a, bb = u0.clone().requires_grad_(True), kap.clone().requires_grad_(True)
+    u = a
+    for _ in range(steps):
+        acc = None
+        for d in range(3):
+            for sh in (-1, 1):
+                un, kn = torch.roll(u, -sh, d), torch.roll(bb, -sh, d)
+                term = (bb + kn) * (un - u)
+                acc = term if acc is None else acc + term
+        u = u + dt * acc
+    loss = ((u - tgt) ** 2).mean()
+    loss.backward()
+    return float(loss.detach())
+
+
+def run_cpu(workload: str, n: int, steps: int) -> dict:
     cores = os.cpu_count() or 1
     env = dict(os.environ, OMP_NUM_THREADS=str(cores), OMP_PROC_BIND="close")
-    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-sample", str(steps), "--n", str(n)]
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-sample", str(steps), "--cpu-workload", workload,
+           "--n", str(n)]
     out = subprocess.run(cmd, env=env, capture_output=True, text=True, check=True).stdout.strip().splitlines()[-1]
     r = json.loads(out)
-    r["cores"] = cores
+    r["cores"] = r.get("threads", cores)
     return r
 
 
+def bounded_steps(workload: str, n: int, seconds: float, cap: int) -> dict:
+    """Run one step to calibrate, then as many steps as fit in ``seconds``."""
+    probe = run_cpu(workload, n, 1)
+    steps = max(1, min(cap, int(math.ceil(seconds / max(probe["seconds"], 1e-3)))))
+    return run_cpu(workload, n, steps)
+
+
 def cpu_baseline(n: int, seconds: float) -> dict:
-    probe = run_cpu(n, 1)
-    steps = max(2, min(400, int(math.ceil(seconds / max(probe["seconds"], 1e-3)))))
-    r = run_cpu(n, steps)
+    r = bounded_steps("cavity", n, seconds, 400)
     lups = SWEEPS_PER_STEP * n * n * r["steps"]
     return {"value": lups / r["seconds"] / 1e9, "unit": "GLUP/s", "cores": r["cores"], "kind": r["kind"],
             "sample": f"cavity {n}x{n} FP64, {r['steps']} steps ({r['seconds']:.1f} s), OpenMP on all host cores"}
@@ -286,6 +366,50 @@ def fp64_peak(n: int = 2048, calls: int = 10) -> float:
     return workloads.FP64_PROBE_ADDS * n * n * calls / (e0.elapsed_time(e1) * 1e-3)
 
 
+def graph_launch_times(native_k, step, flush=None, rounds: int = 3):
+    """({profiling site: [ms, ...]}, steps): the duration of every launch of ``step`` inside
+    the CUDA graphs the timed region replays.  The kernel's graphs are captured
+    again with profiling in graph-node mode (an event-record node before and after
+    every launch); each replay records those events again.  A step may cycle
+    through several graph keys (time levels and scratch buffers rotate), so the
+    steps run until no new graph is captured, then ``rounds`` times that many
+    replays, reading the events after each full cycle.  The kernel's graphs are
+    dropped afterwards (the ones without event nodes are captured again)."""
+    from xgrid_gb300 import device, runtime
+    lib = runtime.load()
+    lib.xg_graph_count.restype = ctypes.c_int64
+    s = device.stream()
+    lib.xg_graph_clear(ctypes.c_void_p(native_k.fn_ptr))
+    lib.xg_prof_reset()
+    lib.xg_prof_enable(2)
+    counts, period = [], 0
+    for _ in range(128):
+        step()
+        counts.append(int(lib.xg_graph_count()))
+        grown = [i for i in range(1, len(counts)) if counts[i] > counts[i - 1]]
+        if grown and counts[-1] == counts[-2] and len(grown) == counts[-1] - counts[0]:
+            period = counts[-1] - counts[0]
+            break
+    s.synchronize()
+    lib.xg_prof_enable(0)
+    if period == 0:
+        raise RuntimeError("the step's graphs did not settle into a cycle")
+    for _ in range(period - 1):  # finish the cycle that the last call started
+        step()
+    by_site: dict = {}
+    for _ in range(rounds):
+        for _ in range(period):
+            if flush is not None:
+                flush()
+            step()
+        s.synchronize()
+        for g, ms in runtime.prof_records():
+            by_site.setdefault(g, []).append(ms)
+    lib.xg_graph_clear(ctypes.c_void_p(native_k.fn_ptr))
+    lib.xg_prof_reset()
+    return by_site, rounds * period
+
+
 # FP64 operations per cell of the cavity's Jacobi sweep after host hoisting: 3 additions and 1
 # subtraction; the products by dx^2, dy^2 and the quotient by 2(dx^2+dy^2) are exact exponent
 # arithmetic on the integer pipe when dx = dy = 2/(n-1) is a power of two (n = 2^k + 1).
@@ -303,7 +427,7 @@ def gpu_bench(args, rank: int, world: int):
 
     torch.cuda.set_device(rank % max(torch.cuda.device_count(), 1))
     cache = JIT_CACHE
-    xgrid.init(precision="double", cacheroot=cache, opt_level=3)
+    xgrid.init(precision="double", cacheroot=cache, opt_level=3, persistent=args.persistent)
     n = args.n
     grids, cfg = workloads.cavity_setup(n, stable_dt(n))
     kern = workloads.cavity_kernel
@@ -348,23 +472,15 @@ def gpu_bench(args, rank: int, world: int):
     secs = replica_time(secs, world)
     lups_rank = SWEEPS_PER_STEP * n * n * args.steps
 
-    # profiled pass (eager, CUDA events around every launch)
+    # launch durations inside the timed region's CUDA graphs (event-record nodes)
     native_k = kern.native
-    native_k.use_graph = False
-    lib.xg_prof_reset()
-    lib.xg_prof_enable(1)
-    prof_steps = min(args.steps, 10)
-    for _ in range(prof_steps):
-        step()
-    s.synchronize()
-    lib.xg_prof_enable(0)
-    recs = runtime.prof_records()
-    launches_per_step = len(recs) / prof_steps
-    lib.xg_prof_reset()
-    native_k.use_graph = True
-    by_site = {}
-    for g, ms in recs:
-        by_site.setdefault(g, []).append(ms)
+
+    def flush_l2():
+        with torch.cuda.stream(s):
+            flush.add_(1)
+
+    by_site, prof_steps = graph_launch_times(native_k, step, flush_l2)
+    launches_per_step = sum(len(v) for v in by_site.values()) / prof_steps
     dom_site, dom_ms = max(by_site.items(), key=lambda kv: sum(kv[1]))
     dom_avg_s = statistics.mean(dom_ms) / 1000.0
     total_prof = sum(sum(x) for x in by_site.values())
@@ -385,7 +501,7 @@ def gpu_bench(args, rank: int, world: int):
         fp64 = {"bound": "fp64 pipe", "achieved_gops": rate64 / 1e9, "peak_gops": peak64 / 1e9,
                 "frac": rate64 / peak64, "ops_per_cell": JACOBI_FP64_OPS,
                 "peak_source": "32-addition FP64 probe sweep measured in this run (L2-resident 2048^2)"}
-        xgrid.init(precision="double", cacheroot=cache, opt_level=3)
+        xgrid.init(precision="double", cacheroot=cache, opt_level=3, persistent=args.persistent)
 
     # e2e through the public API with host buffers
     for g in (u, v, p):
@@ -419,7 +535,8 @@ def gpu_bench(args, rank: int, world: int):
         "data": "synthetic: zero initial fields, lid u=1 (deterministic)",
         "config": {"workload": workload_name(n), "parity": "bit-exact vs the reference's C",
                    "n": n, "sweeps_per_step": SWEEPS_PER_STEP, "l2": "flushed between steps (256 MiB write)",
-                   "parallelism": f"replicas x{world}", "graph": True, "launches_per_step": launches_per_step,
+                   "parallelism": f"replicas x{world}", "graph": True, "persistent_loop": bool(args.persistent),
+                   "launches_per_step": launches_per_step,
                    "tilings": tilings},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "traffic_source": traffic_src,
@@ -434,6 +551,90 @@ def gpu_bench(args, rank: int, world: int):
         "clocks": clk.summary(),
     }
     return result
+
+
+def diffusion_section(n: int = 512, steps: int = 500, runs: int = 3, cpu_seconds: float = 5.0) -> dict:
+    """2-D FTCS diffusion, n^2 FP64, ``steps`` calls of the diffusion kernel per
+    run (the reference's program, one call per time step).  ``value``: device
+    time of a run (L2 flushed before each run; the 4 MB of levels then live in
+    L2 for the run); ``roofline``: the fused sweep + boundary launch at 16
+    algorithmic bytes per cell, its duration from event nodes inside the replayed
+    graphs; ``e2e``: a run through the public API from a host array to a host
+    array; ``parity``: SHA-256 of both levels after the first run of ``steps``
+    steps from the seeded field against the reference's own digests; CPU
+    baseline: the reference's generated C on all host cores."""
+    import hashlib
+
+    import numpy as np
+    import torch
+
+    import xgrid
+    import workloads
+    from xgrid_gb300 import device
+    from xgrid_gb300.operator import Operator
+
+    xgrid.init(precision="double", cacheroot=JIT_CACHE, opt_level=3)
+    k = Operator(workloads.diffusion2d.func, "kernel", "diffusion2d")
+    u, c = workloads.diffusion_setup(n, seed=0)
+    u0 = u.read(0)
+    for _ in range(steps):
+        k(u, c)
+    digests = [hashlib.sha256(u.read(lv).tobytes()).hexdigest() for lv in range(2)]
+    parity = None
+    try:
+        ref = json.load(open(os.path.join(ROOT, "tests", "golden", "full_digests.json")))["diffusion_512"]
+        if n == 512 and steps == 500:
+            parity = "bit-exact vs the reference's digests" if digests == ref["u"] else "MISMATCH"
+    except (OSError, KeyError, ValueError):
+        pass
+    s = device.stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    evs = []
+    for _ in range(runs):
+        with torch.cuda.stream(s):
+            flush.add_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(steps):
+            k(u, c)
+        e1.record(s)
+        evs.append((e0, e1))
+    s.synchronize()
+    run_s = statistics.median(a.elapsed_time(b) for a, b in evs) / 1e3
+    lups = n * n * steps
+    by_site, _ = graph_launch_times(k.native, lambda: k(u, c))
+    dom_site, dom_ms = max(by_site.items(), key=lambda kv: sum(kv[1]))
+    kern_s = statistics.mean(dom_ms) / 1e3
+    hbm, src = peaks()
+    alg = 16.0 * n * n
+    # end to end: host array in, ``steps`` calls, host array out
+    e2e_t = []
+    for _ in range(runs):
+        t0 = time.perf_counter()
+        u.now[...] = u0
+        for _ in range(steps):
+            k(u, c)
+        np.asarray(u.now).sum()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_t)
+    cpu = bounded_steps("diffusion", n, cpu_seconds, steps)
+    return {
+        "config": f"2-D FTCS diffusion {n}x{n} FP64, u0 ~ U[0,1) seed 0, c = 0.2, zero edges, {steps} steps "
+                  f"(one kernel call per step, graph replay per call)",
+        "value": lups / run_s / 1e9, "unit": "GLUP/s", "ms_per_run": run_s * 1e3, "steps_per_run": steps,
+        "parity": parity,
+        "roofline": {"bound": "hbm", "achieved": alg / kern_s / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": alg / kern_s / 1e9 / hbm, "peak_source": src, "kernel_ms": kern_s * 1e3,
+                     "algorithmic_bytes_per_launch": alg,
+                     "note": "levels (4 MB) are L2-resident during a run; launch-latency bound"},
+        "e2e": {"value": lups / e2e_s / 1e9, "unit": "GLUP/s", "h2d_bytes_per_step": n * n * 8,
+                "d2h_bytes_per_step": n * n * 8, "ms_per_run": e2e_s * 1e3,
+                "step": f"one run of {steps} time steps from a host array to a host array"},
+        "cpu_baseline": {"value": n * n * cpu["steps"] / cpu["seconds"] / 1e9, "unit": "GLUP/s",
+                         "cores": cpu["cores"], "kind": cpu["kind"],
+                         "sample": f"diffusion {n}x{n} FP64, {cpu['steps']} steps ({cpu['seconds']:.2f} s), "
+                                   f"OpenMP on all host cores"},
+    }
 
 
 def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
@@ -452,13 +653,14 @@ def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
     from xgrid_gb300.operator import Operator
 
     dt = stable_dt(n)
-    out, fields = {}, {}
+    out, fields, kernels = {}, {}, {}
     for mode in (None, "fp32", "fp16", "bf16"):
         xgrid.init(precision="double", cacheroot=JIT_CACHE,
                    opt_level=3, mixed=mode, mixed_temporal=temporal)
         k = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
         grids, cfg = workloads.cavity_setup(n, dt)
         args = (grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+        kernels[mode] = (k, args, grids)
         half = steps // 2
         for _ in range(steps - half):
             k(*args)
@@ -511,6 +713,43 @@ def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
                       "l2_rel": float(np.linalg.norm(a - ref) / np.linalg.norm(ref))}
         out[mode]["error_vs_fp64"] = err
         out[mode]["speedup_vs_fp64"] = out["fp64"]["ms_per_step"] / out[mode]["ms_per_step"]
+    # dominant kernels inside the replayed graphs: the plain FP64 Jacobi launch and the
+    # temporally blocked FP32 defect launch (12 algorithmic bytes per cell: d and r in, d out)
+    hbm_peak, src = peaks()
+    rl = {}
+    for mode, tag, bpc in ((None, "fp64_jacobi", 24.0), ("fp32", "fp32_defect", 12.0)):
+        k, args, _ = kernels[mode]
+        by_site, nsteps = graph_launch_times(k.native, lambda: k(*args))
+        site, ms = max(by_site.items(), key=lambda kv: sum(kv[1]))
+        ks = statistics.mean(ms) / 1e3
+        rl[tag] = {"bound": "hbm", "achieved": bpc * n * n / ks / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                   "frac": bpc * n * n / ks / 1e9 / hbm_peak, "peak_source": src, "kernel_ms": ks * 1e3,
+                   "site": site, "launches_per_step": len(ms) / nsteps,
+                   "algorithmic_bytes_per_launch": bpc * n * n,
+                   "share_of_step": sum(ms) / sum(sum(v) for v in by_site.values())}
+    out["roofline"] = rl
+    # end to end through the public API, FP32 mode: u, v, p read back to the host every
+    # step and uploaded again by the next call
+    k, args, grids = kernels["fp32"]
+    for g in "puv":
+        grids[g].now  # noqa: B018 - host copies current and authoritative
+    e2e_steps = 10
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        k(*args)
+        for g in "puv":
+            grids[g].now  # noqa: B018
+    device.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    lb = n * n * 8
+    out["e2e"] = {"value": SWEEPS_PER_STEP * n * n / e2e_s / 1e9, "unit": "GLUP/s", "mode": "fp32",
+                  "h2d_bytes_per_step": 3 * lb, "d2h_bytes_per_step": 3 * lb, "ms_per_step": e2e_s * 1e3,
+                  "steps": e2e_steps}
+    cpu = bounded_steps("cavity", n, 8.0, 3)
+    out["cpu_baseline"] = {"value": SWEEPS_PER_STEP * n * n * cpu["steps"] / cpu["seconds"] / 1e9, "unit": "GLUP/s",
+                           "steps_per_s": cpu["steps"] / cpu["seconds"], "cores": cpu["cores"], "kind": cpu["kind"],
+                           "sample": f"cavity {n}x{n} FP64, {cpu['steps']} steps ({cpu['seconds']:.1f} s) of the "
+                                     f"{steps}-step run, extrapolated; OpenMP on all host cores"}
     out["config"] = (f"cavity {n}x{n}, dt={dt:g}, {steps} steps from zero fields; defect iterations in FP32 "
                      f"arithmetic ({temporal} per launch, TMA-staged tiles; fp16/bf16: 16-bit storage with a "
                      f"power-of-two scale per field), FP64 source, residual, correction and projection; one "
@@ -577,16 +816,45 @@ def batch_section(count: int, steps: int, seq_steps: int) -> dict:
     out["batched"]["hbm_frac"] = out["batched"]["gbs"] / hbm
     out["one_step_per_launch"]["hbm_frac"] = out["one_step_per_launch"]["gbs"] / hbm
     out["speedup_vs_per_problem"] = ms_s / ms_b
+    # the batched kernel: one launch advances every tile ``depth`` steps; algorithmic bytes
+    # count 8 per cell and step (read and write one FP32 level), no temporal reuse
+    out["roofline"] = {"bound": "hbm", "achieved": out["batched"]["gbs"], "peak": hbm, "unit": "GB/s",
+                       "frac": out["batched"]["hbm_frac"], "peak_source": src,
+                       "kernel_ms": ms_b / (steps / temporal[0]),
+                       "algorithmic_bytes_per_launch": 8.0 * cells * temporal[0],
+                       "note": f"whole call = {steps // temporal[0]} launches in one CUDA graph"}
+    # end to end: every problem's field from a host array, ``steps`` steps, back to the host
+    host0 = [np.array(p[0].read(0)) for p in probs]
+    t0 = time.perf_counter()
+    for p, h in zip(probs, host0):
+        p[0].now[...] = h
+    k.batch(probs, steps, temporal=temporal)
+    total = 0.0
+    for p in probs:
+        total += float(np.asarray(p[0].now)[0, 0])
+    e2e_s = time.perf_counter() - t0
+    out["e2e"] = {"value": cells * steps / e2e_s / 1e9, "unit": "GLUP/s", "h2d_bytes_per_step": 4 * cells,
+                  "d2h_bytes_per_step": 4 * cells, "ms": e2e_s * 1e3,
+                  "step": f"one call of {steps} steps from host arrays to host arrays"}
+    cpu = bounded_steps("convdiff", 0, 10.0, 50)
+    out["cpu_baseline"] = {"value": cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9, "unit": "GLUP/s",
+                           "cores": cpu["cores"], "kind": cpu["kind"],
+                           "sample": f"reference C, one call per problem per step, {count} squares of the problems' "
+                                     f"cell counts ({cpu['cells']} cells), {cpu['steps']} steps "
+                                     f"({cpu['seconds']:.1f} s); timing only (the reference mis-indexes non-square "
+                                     f"grids), OpenMP on all host cores"}
     out["config"] = (f"{count} problems, extents U[64,1024] per axis (seed 1), FP32, periodic, convection-diffusion "
                      f"5-point, {steps} steps in one CUDA graph of persistent launches")
     return out
 
 
-def adjoint_section(n: int, steps: int, every: int, torch_n: int) -> dict:
+def adjoint_section(n: int, steps: int, every: int, torch_n: int, cpu_n: int = 64) -> dict:
     """3-D variable-coefficient diffusion, FP32, periodic: forward rollout and its
     gradient w.r.t. the initial field and the diffusivity (adjoint kernels with
-    checkpoints every ``every`` steps); PyTorch autograd through the same stencil
-    on tensors at ``torch_n``^3 for comparison."""
+    checkpoints every ``every`` steps).  Compared with PyTorch autograd through
+    the same stencil on tensors: on the GPU at ``torch_n``^3, and on all host
+    cores at ``cpu_n``^3 (the CPU baseline; the reference mis-indexes 3-D grids).
+    ``e2e``: host arrays in, loss gradient arrays out."""
     import numpy as np
     import torch
 
@@ -599,24 +867,33 @@ def adjoint_section(n: int, steps: int, every: int, torch_n: int) -> dict:
                opt_level=3, overstep="wrap")
     k = Operator(workloads.diffuse3d.func, "kernel", "diffuse3d")
 
-    def run_ours(m, nsteps):
+    def run_ours(m, nsteps, host=False):
         u0, kap, tgt, dt = workloads.adjoint_setup(m, 2)
-        u0, kap, tgt = (torch.tensor(x, device="cuda") for x in (u0, kap, tgt))
+        dev = [torch.tensor(x, device="cuda") for x in (u0, kap, tgt)]
         ro = adjoint.Rollout(k, nsteps, every)
-        a, bb = u0.clone().requires_grad_(True), kap.clone().requires_grad_(True)
+        a, bb = dev[0].clone().requires_grad_(True), dev[1].clone().requires_grad_(True)
         s = device.stream()
         # warm-up (compile, tables)
-        ((ro(a, {"k": bb}, (dt,)) - tgt) ** 2).mean().backward()
-        a.grad = None
-        bb.grad = None
+        ((ro(a, {"k": bb}, (dt,)) - dev[2]) ** 2).mean().backward()
         torch.cuda.synchronize()
         s.synchronize()
         t0 = time.perf_counter()
+        if host:  # from host arrays: upload, rollout, gradient, gradients back to the host
+            a = torch.from_numpy(u0).cuda().requires_grad_(True)
+            bb = torch.from_numpy(kap).cuda().requires_grad_(True)
+            tg = torch.from_numpy(tgt).cuda()
+        else:
+            a.grad = None
+            bb.grad = None
+            tg = dev[2]
         uT = ro(a, {"k": bb}, (dt,))
         s.synchronize()
         t1 = time.perf_counter()
-        loss = ((uT - tgt) ** 2).mean()
+        loss = ((uT - tg) ** 2).mean()
         loss.backward()
+        if host:
+            ga, gk = a.grad.cpu().numpy(), bb.grad.cpu().numpy()
+            float(ga[0, 0, 0] + gk[0, 0, 0])
         torch.cuda.synchronize()
         s.synchronize()
         t2 = time.perf_counter()
@@ -624,41 +901,42 @@ def adjoint_section(n: int, steps: int, every: int, torch_n: int) -> dict:
 
     f, bwd, loss = run_ours(n, steps)
     cells = n ** 3
+    hbm, src = peaks()
     out = {"config": f"{n}^3 FP32 periodic, {steps} steps, checkpoint every {every}, loss MSE to a random target",
            "forward_s": f, "backward_s": bwd, "loss": loss,
            "forward_glups": cells * steps / f / 1e9, "forward_gbs": 12.0 * cells * steps / f / 1e9,
            "backward_glups": cells * steps / bwd / 1e9,
            "backward_note": f"backward = {steps - (steps + every - 1) // every} recomputed forward steps + "
                             f"{steps} adjoint steps (24 B/update)"}
-    # PyTorch autograd through the same stencil (tensors, roll), smaller grid
+    out["roofline"] = {"bound": "hbm", "achieved": out["forward_gbs"], "peak": hbm, "unit": "GB/s",
+                       "frac": out["forward_gbs"] / hbm, "peak_source": src,
+                       "kernel_ms": f / steps * 1e3, "algorithmic_bytes_per_launch": 12.0 * cells,
+                       "note": "forward z-walk kernel, one launch per step (read u, k; write u)"}
+    fh, bh, _ = run_ours(n, steps, host=True)
+    out["e2e"] = {"value": cells * steps / (fh + bh) / 1e9, "unit": "GLUP/s (forward steps / forward+backward time)",
+                  "h2d_bytes_per_step": 3 * 4 * cells, "d2h_bytes_per_step": 2 * 4 * cells,
+                  "s": fh + bh, "step": f"one rollout of {steps} steps and its gradient, host arrays in and out"}
+    # PyTorch autograd through the same stencil on the GPU, smaller grid
     fs, bs, _ = run_ours(torch_n, steps)
     u0, kap, tgt, dt = workloads.adjoint_setup(torch_n, 2)
     u0, kap, tgt = (torch.tensor(x, device="cuda") for x in (u0, kap, tgt))
-
-    def tstep(u, kk):
-        acc = None
-        for d in range(3):
-            for sh in (-1, 1):
-                un, kn = torch.roll(u, -sh, d), torch.roll(kk, -sh, d)
-                term = (kk + kn) * (un - u)
-                acc = term if acc is None else acc + term
-        return u + dt * acc
-
-    def torch_run():
-        a, bb = u0.clone().requires_grad_(True), kap.clone().requires_grad_(True)
-        u = a
-        for _ in range(steps):
-            u = tstep(u, bb)
-        ((u - tgt) ** 2).mean().backward()
-
-    torch_run()
+    torch_autograd_run(u0, kap, tgt, dt, steps)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    torch_run()
+    torch_autograd_run(u0, kap, tgt, dt, steps)
     torch.cuda.synchronize()
     tt = time.perf_counter() - t0
     out["torch_autograd_gpu"] = {"n": torch_n, "fwd_bwd_s": tt, "ours_fwd_bwd_s": fs + bs,
                                  "speedup": tt / (fs + bs)}
+    # CPU baseline: torch autograd on all host cores at cpu_n^3, ours at the same size
+    fc, bc, _ = run_ours(cpu_n, steps)
+    cpu = bounded_steps("adjoint", cpu_n, 10.0, steps)
+    per_step_cpu = cpu["seconds"] / cpu["steps"]
+    out["cpu_baseline"] = {"value": cpu_n ** 3 / per_step_cpu / 1e9, "unit": "GLUP/s (forward steps / fwd+bwd time)",
+                           "cores": cpu["cores"], "kind": cpu["kind"],
+                           "sample": f"torch CPU autograd through the same stencil, {cpu_n}^3 FP32, {cpu['steps']} "
+                                     f"steps forward + backward ({cpu['seconds']:.1f} s), {cpu['cores']} threads",
+                           "ours_same_size_value": cpu_n ** 3 * steps / (fc + bc) / 1e9}
     return out
 
 
@@ -685,11 +963,11 @@ def reference_arm(args, rank: int, world: int):
     if rank != 0:
         return None
     n = args.n
-    probe = run_cpu(n, 1)
+    probe = run_cpu("cavity", n, 1)
     per_step = max(1, int(math.ceil(args.cpu_seconds / 10 / max(probe["seconds"], 1e-3))))
     per_step = min(per_step, 5)
-    run_cpu(n, max(1, args.warmup))
-    r = run_cpu(n, args.steps * per_step if args.steps * per_step * probe["seconds"] < 240 else
+    run_cpu("cavity", n, max(1, args.warmup))
+    r = run_cpu("cavity", n, args.steps * per_step if args.steps * per_step * probe["seconds"] < 240 else
                 max(1, int(240 / max(probe["seconds"], 1e-3))))
     lups = SWEEPS_PER_STEP * n * n * r["steps"]
     val = lups / r["seconds"] / 1e9
@@ -708,7 +986,7 @@ def reference_arm(args, rank: int, world: int):
 def main():
     args = parse_args()
     if args.cpu_sample:
-        print(json.dumps(cpu_sample(args.n, args.cpu_sample)))
+        print(json.dumps(cpu_sample(args.cpu_workload, args.n, args.cpu_sample)))
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -725,6 +1003,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
     out = gpu_bench(args, rank, world)
+    if rank == 0 and not args.no_diffusion:
+        out["diffusion"] = diffusion_section(512, 500)
     if rank == 0 and not args.no_mixed:
         out["mixed"] = mixed_section(args.mixed_n, args.mixed_steps, args.mixed_temporal)
     if rank == 0 and not args.no_batch:

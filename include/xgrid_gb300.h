@@ -136,6 +136,13 @@ int xg_mask_tiles(xg_mask* mask, const int32_t* tile, int32_t value,
  * lies in the same tile as c (reads outside the grid count as local). */
 int xg_mask_tile_local(xg_mask* mask, const int32_t* tile, int32_t value, int noff,
                        const int32_t* offsets, int overstep, int* ok);
+/* 1 in *ok when every read of a mask-0 cell at one of the `noff` offsets (noff x 3,
+ * order z,y,x) under `overstep` lands in the cell's tile or in a tile next to it
+ * (along each axis at most one tile away, wrapped across the grid under "wrap"):
+ * the condition under which a persistent loop launch lets each tile wait only for
+ * its neighbouring tiles.  Reads outside the allocation count as local. */
+int xg_mask_tile_reach(xg_mask* mask, const int32_t* tile, int noff, const int32_t* offsets, int overstep,
+                       int* ok);
 /* Box tables of temporally blocked launches (runtime helpers with no
  * counterpart in the reference, which sweeps once per statement).  Tiles have
  * exactly core = {tz, ty, tx} cells (the last tile of an axis may reach past
@@ -189,8 +196,11 @@ int xg_wide_index_forced(void);
 /* Generated modules call xg_prof_launch() before every kernel launch and
  * xg_prof_end() after it.  Both only count unless profiling is on; with
  * profiling on, CUDA events are recorded around each launch on its stream and
- * xg_prof_read() returns (group id, milliseconds) per launch.  Profiling is for
- * eager calls only (a captured graph records no events). */
+ * xg_prof_read() returns (group id, milliseconds) per launch.  A call captured
+ * into a CUDA graph while profiling is on gets its events as event-record nodes
+ * of the graph: each replay records them again, and xg_prof_read() then returns
+ * the durations of the launches of the latest replay.  xg_prof_enable(2) records
+ * only launches that are being captured (graph nodes), xg_prof_enable(1) all. */
 void xg_prof_enable(int on);
 int xg_prof_enabled(void);
 void xg_prof_launch(int group, void* stream);

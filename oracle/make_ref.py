@@ -2,9 +2,11 @@
 
 Needs the reference checkout: argv[1] or the environment variable
 ``XGRID_REFERENCE``.  For each of
-the two benchmark programs in workloads.py (2-D diffusion, lid-driven cavity)
-it runs the reference's parser and C generator (xgrid/lang/generator.py) and
-writes the C source to oracle/_ref/<kernel>.c.  Those files are not versioned;
+the benchmark programs in workloads.py (2-D diffusion and the lid-driven cavity
+in FP64, the batched convection-diffusion step in FP32 with periodic edges) it
+runs the reference's parser and C generator (xgrid/lang/generator.py), under the
+configuration that program runs with, and writes the C source to
+oracle/_ref/<kernel>.c.  Those files are not versioned;
 they travel with the working tree and ``oracle.native.build_ref`` compiles them
 with the reference's compiler flags on whatever host runs the baseline.
 """
@@ -16,7 +18,9 @@ import tempfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_ref")
-KERNELS = ("diffusion2d", "cavity_kernel")
+# kernel -> (precision, overstep) it is generated under
+KERNELS = {"diffusion2d": ("double", "none"), "cavity_kernel": ("double", "none"),
+           "convdiff2d": ("float", "wrap")}
 
 CHILD = r"""
 import os, sys
@@ -24,11 +28,14 @@ sys.path.insert(0, {ref!r})
 sys.path.insert(1, {root!r})
 import xgrid
 assert os.path.abspath(xgrid.__file__).startswith(os.path.abspath({ref!r}))
-xgrid.init(parallel=True, precision="double", opt_level=3, cacheroot=".xgridref")
 import workloads
 from xgrid.lang.generator import Generator
-for name in {kernels!r}:
-    src = Generator(getattr(workloads, name)).source
+for name, (precision, overstep) in {kernels!r}.items():
+    # the parser fixes the width of float when it first reads a kernel, so each
+    # kernel gets a fresh operator under its own configuration
+    xgrid.init(parallel=True, precision=precision, overstep=overstep, opt_level=3, cacheroot=".xgridref")
+    op = getattr(workloads, name)
+    src = Generator(xgrid.kernel()(op.func)).source
     with open(os.path.join({out!r}, name + ".c"), "w") as f:
         f.write(src)
 """

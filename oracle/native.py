@@ -75,7 +75,7 @@ def ref_sources() -> list:
 
 
 def ref_available() -> bool:
-    return all(os.path.exists(os.path.join(REF, k + ".so")) for k in ("diffusion2d", "cavity_kernel"))
+    return all(os.path.exists(os.path.join(REF, k + ".so")) for k in ("diffusion2d", "cavity_kernel", "convdiff2d"))
 
 
 # ------------------------------------------------------------------ drivers
@@ -91,7 +91,16 @@ class RefGrid2d(ctypes.Structure):
                 ("boundary_mask", ctypes.POINTER(ctypes.c_int32))]
 
 
+class RefGrid2dF(ctypes.Structure):
+    """``struct __Grid2d_f`` of the reference's generated C (FP32 levels)."""
+
+    _fields_ = [("time", ctypes.c_int32), ("shape", ctypes.c_int32 * 2),
+                ("data", ctypes.POINTER(ctypes.POINTER(ctypes.c_float))),
+                ("boundary_mask", ctypes.POINTER(ctypes.c_int32))]
+
+
 _DP = ctypes.POINTER(ctypes.c_double)
+_FP = ctypes.POINTER(ctypes.c_float)
 _IP = ctypes.POINTER(ctypes.c_int32)
 
 
@@ -124,6 +133,46 @@ class Field:
         g.data = ctypes.cast(self._ptrs, ctypes.POINTER(_DP))
         g.boundary_mask = _ip(self.mask)
         return g
+
+
+class Field32:
+    """Two FP32 time levels and a mask (the batched program), rotated like Field."""
+
+    def __init__(self, level0: np.ndarray, mask=None) -> None:
+        level0 = np.ascontiguousarray(level0, dtype=np.float32)
+        self.levels = [level0.copy(), np.zeros_like(level0)]
+        self.mask = np.zeros(level0.shape, np.int32) if mask is None else np.ascontiguousarray(mask, np.int32)
+        self._ptrs = None
+
+    def tick(self) -> None:
+        self.levels.insert(0, self.levels.pop())
+
+    def ref_struct(self) -> RefGrid2dF:
+        g = RefGrid2dF()
+        g.time = len(self.levels)
+        g.shape[0], g.shape[1] = self.levels[0].shape
+        self._ptrs = (_FP * len(self.levels))(*[x.ctypes.data_as(_FP) for x in self.levels])
+        g.data = ctypes.cast(self._ptrs, ctypes.POINTER(_FP))
+        g.boundary_mask = _ip(self.mask)
+        return g
+
+
+def convdiff_reference(exact: bool = False):
+    """The reference's generated C of the batched program (FP32, periodic):
+    ``fn(Field32, (a0, axm, axp, aym, ayp), steps)``.  Square grids only: the
+    reference strides non-square grids by the wrong extent."""
+    path = os.path.join(REF, "convdiff2d" + (".exact.so" if exact else ".so"))
+    if not os.path.exists(path):
+        build_ref()
+    lib = ctypes.CDLL(path)
+    lib.convdiff2d.argtypes = [RefGrid2dF] + [ctypes.c_float] * 5
+    lib.convdiff2d.restype = None
+
+    def run(field: Field32, coeffs, steps: int) -> None:
+        for _ in range(steps):
+            field.tick()
+            lib.convdiff2d(field.ref_struct(), *coeffs)
+    return run
 
 
 class Oracle:

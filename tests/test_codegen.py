@@ -62,13 +62,15 @@ def test_mixed_loop_has_temporal_tma_kernel():
 
 def test_persistent_loop_kernel_for_in_place_loops():
     """The cavity pressure loop (implicit Jacobi sweep + four boundary sweeps) gets
-    a persistent loop launch: a cooperative launch, the grid barrier between
-    iterations, level and scratch alternating by iteration parity; a loop whose
-    body uses the loop variable or writes two grids does not."""
+    a persistent loop launch: a cooperative launch, each tile waiting for its
+    neighbouring tiles' completion flags (zeroed by a memset before the launch),
+    level and scratch alternating by iteration parity; a loop whose body uses the
+    loop variable or writes two grids does not."""
     m = _gen(workloads.cavity_kernel, persistent=True)
     assert "xgk_cavity_kernel_1_loop" in m.source
     assert "cudaLaunchAttributeCooperative" in m.source
-    assert "xg_grid_sync(p.sync" in m.source and "xg_grid_exit(p.sync" in m.source
+    assert "xg_tile_wait(p.flags, xg_tt" in m.source and "xg_tile_done(p.flags, xg_tt" in m.source
+    assert "cudaMemsetAsync(p.flags, 0" in m.source and "xg_mask_tile_reach(" in m.source
     assert "(xg_it & 1) ? p.b1_0_1 : p.b1_0_0" in m.source
     assert m.source.count("_loop(xg_G, &xg_h, xg_K, xg_s)") == 1
     off = _gen(workloads.cavity_kernel)

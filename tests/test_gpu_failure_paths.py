@@ -1,7 +1,7 @@
 """The device-side waits that can give up do so without a hang or a fault, and
 report it.  Modules compiled with ``xgrid.init(fail_waits=True)`` make those
-waits unable to succeed: the grid barrier of a persistent loop launch polls
-once, and the TMA staging barrier of the temporally blocked mixed-precision
+waits unable to succeed: the neighbour-tile wait of a persistent loop launch
+polls once, and the TMA staging barrier of the temporally blocked mixed-precision
 kernel expects more bytes than its copies deliver.  Each call must return,
 its error word must read 1 (``loop_error`` / ``staging_error``), clearing must
 reset it, and afterwards a regular module on the same context must still give
@@ -51,11 +51,11 @@ def _context_still_usable(cacheroot):
     assert out[0].tobytes() == out[1].tobytes()
 
 
-def test_grid_barrier_gives_up_and_reports(cacheroot):
+def test_tile_wait_gives_up_and_reports(cacheroot):
     xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3, persistent=True, fail_waits=True)
-    k = Operator(relax, "kernel", "relax_fail_barrier")
+    k = Operator(relax, "kernel", "relax_fail_tile_wait")
     p, f = _grids(xgrid, 512, 3)
-    k(p, f, 20, 1e-3)          # returns: every CTA leaves at its first barrier that does not complete
+    k(p, f, 20, 1e-3)          # returns: a CTA leaves at its first neighbour wait that does not succeed
     device.synchronize()
     assert k.native.loop_error() == 1
     assert k.native.loop_error(clear=True) == 1

@@ -1,7 +1,7 @@
 """Temporally blocked defect iterations of the mixed-precision pressure loop
 (TMA-staged boxes, several iterations per launch).  With FP32 storage the
 result has the same bits as one iteration per launch, for every depth and
-strip height, on square and non-square grids with odd extents; with 16-bit
+box height (rows per warp), on square and non-square grids with odd extents; with 16-bit
 storage (FP16 / BF16 and a power-of-two scale per field) the pressure stays
 within the storage format's tolerance of the FP64 path.  The staging copies
 never time out (error word of the work area stays 0)."""
@@ -42,7 +42,7 @@ def kernel(cacheroot, mode):
     return Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
 
 
-def run(k, shape, steps, temporal, rows=16, dt=1e-5):
+def run(k, shape, steps, temporal, rows=8, dt=1e-5):
     if k.native is None:
         from xgrid_gb300.native import NativeKernel
         k.native = NativeKernel(k)
@@ -60,7 +60,7 @@ def run(k, shape, steps, temporal, rows=16, dt=1e-5):
 
 
 @pytest.mark.parametrize("shape", [(257, 257), (203, 333)])
-@pytest.mark.parametrize("temporal,rows", [(4, 16), (3, 8), (1, 16), (6, 16), (8, 24)])
+@pytest.mark.parametrize("temporal,rows", [(4, 8), (3, 4), (1, 8), (6, 8), (8, 4), (8, 8)])
 def test_fp32_temporal_equals_one_iteration_per_launch(cacheroot, shape, temporal, rows):
     k = kernel(cacheroot, "fp32")
     ref, n_ref, _ = run(k, shape, 6, 0)
@@ -124,7 +124,7 @@ def test_box_check_accepts_and_rejects(cacheroot, column, temporal_used):
     lib = runtime.load()
     out, launches = {}, {}
     for T in (0, 4):
-        k.native.set_mixed_temporal(T, 16)
+        k.native.set_mixed_temporal(T, 8)
         rng = np.random.default_rng(7)
         p, f = xgrid.Grid((300, 300), float), xgrid.Grid((300, 300), float)
         p.now[...] = rng.random((300, 300))

@@ -1,10 +1,11 @@
 """Persistent loop launches (``xgrid.init(persistent=True)``): an
 in-place loop whose body is one implicit main sweep and its boundary sweeps runs
-as one cooperative launch with a grid barrier between iterations.  The results
+as one cooperative launch in which each tile waits only for its neighbouring
+tiles' previous iteration.  The results
 are the same bits as one launch per iteration, for odd and even iteration
 counts (the level/scratch exchange parity), 2-D and 3-D grids, extents that are
 not multiples of the tile, and against the oracle.  A loop whose boundary cells
-read cells of another tile falls back to one launch per iteration.  No barrier
+read cells of another tile falls back to one launch per iteration.  No tile
 wait ever gives up (error word 0)."""
 import numpy as np
 import pytest

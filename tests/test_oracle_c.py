@@ -39,3 +39,25 @@ def test_c_oracle_matches_reference_generated_c(n, steps):
         out.append(f)
     for k in "bpuv":
         assert out[0][k].levels[0].tobytes() == out[1][k].levels[0].tobytes()
+
+
+@pytest.mark.skipif(not (native.ref_available() or native.ref_sources()),
+                    reason="the reference's generated C is not present (oracle/make_ref.py writes it)")
+def test_reference_generated_convdiff_matches_reference_digests():
+    """The batched program's reference C (the CPU baseline of the batched workload)
+    reproduces the reference package's own digests on square periodic FP32 grids."""
+    import hashlib
+    import json
+    dig = json.load(open(os.path.join(HERE, "full_digests.json")))["convdiff_square"]
+    rng = np.random.default_rng(5)
+    run = native.convdiff_reference(exact=True)
+    for n in (64, 257, 512):
+        cx, cy = (float(v) for v in rng.uniform(-1.0, 1.0, 2))
+        nu = float(rng.uniform(0.01, 0.1))
+        dx = 1.0 / n
+        dt = 0.2 * dx * dx / nu
+        gx, gy = 0.5 * cx * dt / dx, 0.5 * cy * dt / dx
+        k = nu * dt / (dx * dx)
+        f = native.Field32(rng.random((n, n)).astype(np.float32))
+        run(f, (1.0 - 4.0 * k, gx + k, k - gx, gy + k, k - gy), 200)
+        assert [hashlib.sha256(np.ascontiguousarray(x).tobytes()).hexdigest() for x in f.levels] == dig[f"u{n}"]

@@ -167,24 +167,35 @@ def convdiff2d(u: float2d, a0: float, axm: float, axp: float, aym: float, ayp: f
     u[0, 0] = a0 * u[0, 0] + axm * u[0, -1] + axp * u[0, 1] + aym * u[-1, 0] + ayp * u[1, 0]
 
 
-def batch_setup(count: int = 256, seed: int = 1, lo: int = 64, hi: int = 1024):
+def batch_params(count: int = 256, seed: int = 1, lo: int = 64, hi: int = 1024):
     """``count`` periodic FP32 problems: extents uniform in [lo, hi] per axis,
     velocities c ~ U[-1, 1], nu ~ U[0.01, 0.1], u0 ~ U[0, 1), dt from the CFL and
-    diffusion limits; returns the argument tuples of ``convdiff2d``."""
+    diffusion limits; returns ``(u0, coefficients)`` per problem, the
+    coefficients being the scalar arguments of ``convdiff2d``."""
     rng = np.random.default_rng(seed)
-    problems = []
+    out = []
     for _ in range(count):
         ny, nx = (int(v) for v in rng.integers(lo, hi + 1, 2))
         cx, cy = (float(v) for v in rng.uniform(-1.0, 1.0, 2))
         nu = float(rng.uniform(0.01, 0.1))
         dx, dy = 1.0 / nx, 1.0 / ny
         dt = 0.2 * min(dx, dy) ** 2 / nu
-        u = xgrid.Grid((ny, nx), float)
-        u.now[...] = rng.random((ny, nx)).astype(u.numpy_dtype)
+        u0 = rng.random((ny, nx)).astype(np.float32)
         # per-step coefficients: central convection, explicit diffusion
         gx, gy = 0.5 * cx * dt / dx, 0.5 * cy * dt / dy
         kx, ky = nu * dt / (dx * dx), nu * dt / (dy * dy)
-        problems.append((u, 1.0 - 2.0 * kx - 2.0 * ky, gx + kx, kx - gx, gy + ky, ky - gy))
+        out.append((u0, (1.0 - 2.0 * kx - 2.0 * ky, gx + kx, kx - gx, gy + ky, ky - gy)))
+    return out
+
+
+def batch_setup(count: int = 256, seed: int = 1, lo: int = 64, hi: int = 1024):
+    """The problems of ``batch_params`` as argument tuples of ``convdiff2d``
+    (one FP32 grid per problem, ``xgrid.init(precision="float")``)."""
+    problems = []
+    for u0, coeffs in batch_params(count, seed, lo, hi):
+        u = xgrid.Grid(u0.shape, float)
+        u.now[...] = u0.astype(u.numpy_dtype)
+        problems.append((u, *coeffs))
     return problems
 
 

@@ -553,8 +553,8 @@ class CudaGenerator:
         src.append("  return 0;")
         src.append("}")
         src.append(f'extern "C" int xg_mixed_{name}(int64_t every) {{ xg_mixed_every_{name} = every; return 0; }}')
-        # error word of the persistent loops' grid barriers (1: a barrier wait gave up, the
-        # results of that call are invalid); clear = 1 also resets the barrier words
+        # error word of the persistent loops (1: a neighbour-tile wait gave up, the results
+        # of that call are invalid); clear = 1 resets it
         src.append(f'extern "C" int xg_loop_error_{name}(int clear) {{')
         src.append("  int e = 0;")
         for gid in self.loop_groups:
@@ -1406,7 +1406,8 @@ class SweepGroupEmitter:
         """Tile kernel: main sweeps ``mains`` (indices into the group) then the
         boundary phases ``bnd_phases`` on the tile's own cells.  ``loop``: the
         persistent variant, p.K iterations of the group in one cooperative launch
-        (tiles strided over the CTAs, a grid barrier between iterations)."""
+        (tiles strided over the CTAs, each tile waiting for its neighbouring tiles'
+        previous iteration)."""
         n, gid = self.name, self.gid
         sweeps = [self.g.sweeps[j] for j in mains]
         # neighbourhood of the main loads, for the unchecked fast path
@@ -1425,6 +1426,8 @@ class SweepGroupEmitter:
         if loop:
             lines += ["  for (int xg_it = 0; xg_it < (int)p.K; ++xg_it) {",
                       "  for (int xg_tt = blockIdx.x; xg_tt < (int)(p.ntz * p.nty * p.ntx); xg_tt += gridDim.x) {",
+                      "  if (xg_it > 0 && !xg_tile_wait(p.flags, xg_tt, p.ntz, p.nty, p.ntx, p.wrap, (unsigned)xg_it, "
+                      "p.err)) return;",
                       "  const xg_tile T = xg_tile_at(xg_tt, p.Z, p.Y, p.X, p.tz, p.ty, p.tx, p.nty, p.ntx, p.ntz);"]
             lines += TILE_PROLOGUE[1:] + self.loop_locals(members)
         else:
@@ -1493,10 +1496,9 @@ class SweepGroupEmitter:
             lines.append("  }}")
             lines += ["  " + l for l in post]
         if loop:
-            lines += ["  }",
-                      "  if (xg_it + 1 < p.K && !xg_grid_sync(p.sync, gridDim.x, (unsigned)(xg_it + 1))) return;",
+            lines += ["  xg_tile_done(p.flags, xg_tt, (unsigned)(xg_it + 1));",
                       "  }",
-                      "  xg_grid_exit(p.sync, gridDim.x, (unsigned)(p.K - 1));"]
+                      "  }"]
         lines.append("}")
         return "\n".join(lines)
 
@@ -1661,24 +1663,31 @@ class SweepGroupEmitter:
     def emit_loop(self) -> None:
         """Persistent launch of ``K`` iterations of this group (the body of an
         in-place loop): the fused kernel's tile work in a loop over iterations,
-        one cooperative launch of at most the resident CTAs, a grid barrier
-        between iterations.  The launcher returns 1 when it ran, 0 when the
-        launch does not apply (shapes, tile-local boundary reads), so the caller
-        falls back to one launch per iteration."""
+        one cooperative launch of at most the resident CTAs, each tile waiting
+        for its neighbouring tiles' previous iteration (completion flags, zeroed
+        by a memset before the launch).  The launcher returns 1 when it ran, 0
+        when the launch does not apply (shapes, tile-local boundary reads, reads
+        beyond the neighbouring tiles, more tiles than flags), so the caller falls
+        back to one launch per iteration."""
         n, gid = self.name, self.gid
         sweeps = self.g.sweeps
         mains = [j for j, s in enumerate(sweeps) if s.is_main]
         bnds = [j for j, s in enumerate(sweeps) if not s.is_main]
-        extra = ["int64_t K", "unsigned* sync"]
+        extra = ["int64_t K", "unsigned* flags", "unsigned* err", "int wrap"]
         for j in mains:
             extra += [f"const int32_t* m{j}", f"const uint8_t* tzero{j}"]
         for j in bnds:
             extra += [f"const int32_t* bo{j}", f"const int64_t* bc{j}"]
-        self.gen.device_chunks.append(f"__device__ unsigned xg_sync_{n}_{gid}[2] = {{0u, 0u}};")
+        self.gen.device_chunks.append(
+            f"#define XG_LOOP_MAX_TILES_{n}_{gid} 65536\n"
+            f"__device__ unsigned xg_flags_{n}_{gid}[XG_LOOP_MAX_TILES_{n}_{gid}];\n"
+            f"__device__ unsigned xg_sync_{n}_{gid}[2] = {{0u, 0u}};  // [1]: a tile wait gave up")
         self.gen.device_chunks.append(self.params_struct("loop", sweeps, extra))
         self.gen.device_chunks.append(self.main_kernel("loop", mains, bnds, loop=True))
         dom = sweeps[mains[0]].slot
         s0 = sweeps[0]
+        offs = sorted({ld.offset for j in mains for _, ld in sweeps[j].loads})
+        flat = ", ".join(str(v) for o in offs for v in o)
         L = [f"static int xgl_{n}_{gid}_loop(xg_grid* G, const struct xgh_{n}_{gid}* h, int64_t K, cudaStream_t s) {{"]
         L += self.check_levels(sweeps)
         L += self.fill_params("loop", sweeps, dom)
@@ -1692,32 +1701,46 @@ class SweepGroupEmitter:
         for j in bnds:
             sj = sweeps[j]
             L.append(f"  XG_TRY(xg_mask_tiles(G[{sj.slot}].mask, tl, {sj.mask}, NULL, &p.bo{j}, &p.bc{j}, &ntiles));")
-        for j, offs in self.g.local_checks:
+        for j, loffs in self.g.local_checks:
             sj = sweeps[j]
-            flat = ", ".join(str(v) for o in offs for v in o)
-            L += ["  {", f"    static const int32_t offs[] = {{{flat}}};", "    int ok = 0;",
-                  f"    XG_TRY(xg_mask_tile_local(G[{sj.slot}].mask, tl, {sj.mask}, {len(offs)}, offs, "
+            lflat = ", ".join(str(v) for o in loffs for v in o)
+            L += ["  {", f"    static const int32_t offs[] = {{{lflat}}};", "    int ok = 0;",
+                  f"    XG_TRY(xg_mask_tile_local(G[{sj.slot}].mask, tl, {sj.mask}, {len(loffs)}, offs, "
                   f"xg_overstep, &ok));",
                   "    if (!ok) return 0;", "  }"]
-        L += ["  if (ntiles != p.ntz * p.nty * p.ntx) XG_FAIL(\"tile table mismatch\");",
-              "  if (K > 0x7fffffffLL || ntiles > 0x7fffffffLL) return 0;",
+        L += ["  {  // every main-sweep read of a mask-0 cell lands in its tile or a neighbouring tile",
+              f"    static const int32_t offs[] = {{{flat}}};", "    int ok = 0;",
+              f"    XG_TRY(xg_mask_tile_reach(G[{sweeps[mains[0]].slot}].mask, tl, {len(offs)}, offs, xg_overstep, "
+              f"&ok));",
+              "    if (!ok) return 0;", "  }",
+              "  if (ntiles != p.ntz * p.nty * p.ntx) XG_FAIL(\"tile table mismatch\");",
+              f"  if (K > 0x7fffffffLL || ntiles > XG_LOOP_MAX_TILES_{n}_{gid}) return 0;",
               "  p.K = K;",
-              f"  XG_CUDA(cudaGetSymbolAddress((void**)&p.sync, xg_sync_{n}_{gid}));",
+              "  p.wrap = xg_overstep == XG_OVERSTEP_WRAP;",
+              "  int dev = 0, sms = 0;",
+              "  XG_CUDA(cudaGetDevice(&dev));",
+              "  static void* flags_addr[64];",
+              "  static void* sync_addr[64];",
+              "  if (dev < 0 || dev >= 64) return 0;",
+              f"  if (!flags_addr[dev]) XG_CUDA(cudaGetSymbolAddress(&flags_addr[dev], xg_flags_{n}_{gid}));",
+              f"  if (!sync_addr[dev]) XG_CUDA(cudaGetSymbolAddress(&sync_addr[dev], xg_sync_{n}_{gid}));",
+              "  p.flags = (unsigned*)flags_addr[dev];",
+              "  p.err = (unsigned*)sync_addr[dev] + 1;",
               "  const dim3 block(tl[3], tl[4], tl[5]);",
               "  const int threads = tl[3] * tl[4] * tl[5];",
+              "  if (threads < 27) return 0;  // a tile wait polls its neighbours with threads 0..26",
               "  const bool small = xg_small_index(p.Z, p.Y, p.X);",
               "  int per_sm = 0;",
               f"  if (small) XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xgk_{n}_{gid}_loop<int>, "
               "threads, 0));",
               f"  else XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xgk_{n}_{gid}_loop<int64_t>, "
               "threads, 0));",
-              "  int dev = 0, sms = 0;",
-              "  XG_CUDA(cudaGetDevice(&dev));",
               "  XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));",
               "  if (per_sm < 1) return 0;",
               "  const int64_t resident = (int64_t)per_sm * sms;",
               "  const int64_t nb = ntiles < resident ? ntiles : resident;",
               "  if (nb < 1) return 0;",
+              "  XG_CUDA(cudaMemsetAsync(p.flags, 0, (size_t)ntiles * sizeof(unsigned), s));",
               "  cudaLaunchConfig_t lc;",
               "  memset(&lc, 0, sizeof lc);",
               "  cudaLaunchAttribute at[1];",

@@ -26,20 +26,20 @@ Backend options (new keywords, all optional):
 * ``mixed_temporal``: defect iterations per launch of the temporally blocked
   defect kernel (TMA-staged tile + halo in shared memory); 0 runs one iteration
   per launch without shared-memory staging (FP32 storage).
-* ``mixed_rows``: rows per thread of that kernel (8, 16 or 24; the tile is
-  128 columns by twice this many rows, halo included).
+* ``mixed_rows``: rows per warp of that kernel (4 or 8; the box is 128 columns
+  by eight times this many rows, halo included).
 * ``int_adds``: every n-th FP64 addition or subtraction of a sweep runs as an
   exact round-to-nearest integer-pipe routine instead of the FP64 unit (0: none,
   1: all); the results are the same bits, only the pipe balance changes.
 * ``persistent``: run an in-place loop whose body is one launch group (an
   implicit main sweep of a grid and its boundary sweeps, e.g. Jacobi iterations)
-  as one cooperative launch with a grid barrier between iterations, instead of
-  one launch per iteration; same arithmetic, same bits.  Off by default: on a
-  GB300 the grid barrier of ~600 CTAs costs more than a launch boundary inside
-  a CUDA graph (cavity 1025^2: 1.12x the step time).
+  as one cooperative launch in which each tile waits only for its neighbouring
+  tiles' previous iteration (per-tile completion flags), instead of one launch
+  per iteration; same arithmetic, same bits.  Calls of one module with this
+  option must not overlap on the GPU (the flags are a module-wide array).
 * ``fail_waits``: for testing only.  Compile modules whose give-up waits cannot
-  succeed (the grid barrier of a persistent loop polls once; a TMA staging
-  barrier expects more bytes than its copies deliver), so that those waits run
+  succeed (the neighbour-tile wait of a persistent loop polls once; a TMA
+  staging barrier expects more bytes than its copies deliver), so that those waits run
   out: the kernel sets its error word and returns, after draining its copies.
   Results of such modules are invalid by construction.
 * ``graph``: capture each distinct kernel call into a CUDA graph and replay it.
@@ -63,7 +63,7 @@ logger = Logger("xgrid")
 _OVERSTEP = ("none", "limit", "wrap")
 _PRECISION = ("float", "double")
 _MIXED = (None, "fp32", "fp16", "bf16")
-MIXED_ROWS = (8, 16, 24)
+MIXED_ROWS = (4, 8)
 
 
 @dataclasses.dataclass
@@ -83,7 +83,7 @@ class Configuration:
     mixed_every: int = 0
     autotune: bool = True
     mixed_temporal: int = 4
-    mixed_rows: int = 16
+    mixed_rows: int = 8
     int_adds: int = 0
     persistent: bool = False
     fail_waits: bool = False
@@ -119,7 +119,7 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
          opt_level: Literal[0, 1, 2, 3] = 2, precision: Literal["float", "double"] = "float",
          exact: bool = True, mixed: Optional[str] = None, graph: bool = True,
          fuse: bool = True, divisor: bool = True, mixed_every: int = 0, autotune: bool = True,
-         mixed_temporal: int = 4, mixed_rows: int = 16, int_adds: int = 0, persistent: bool = False,
+         mixed_temporal: int = 4, mixed_rows: int = 8, int_adds: int = 0, persistent: bool = False,
          fail_waits: bool = False) -> None:
     """Set the global configuration (same keywords as the reference plus GPU options)."""
     global _config

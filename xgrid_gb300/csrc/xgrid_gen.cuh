@@ -348,11 +348,12 @@ __device__ __forceinline__ void xg_tma_load_2d(void* dst, const CUtensorMap* map
 // Bounded waits.  Every device-side wait gives up after XG_WAIT_NS nanoseconds of
 // the global timer (about a second; the copies and barriers it waits for take
 // microseconds).  The waits whose give-up path reports an error and leaves (the
-// first wait for a TMA staging copy, the grid barrier of a persistent loop) use
-// XG_GIVEUP_NS, the same by default.  A module compiled with XG_FAIL_WAITS makes
-// those waits unable to succeed, to test the give-up paths: the grid barrier polls
-// once, and a TMA staging barrier expects 16 bytes more than its copies deliver
-// (the copies themselves still land, and the CTA drains them before it leaves).
+// first wait for a TMA staging copy, the neighbour-tile wait of a persistent loop)
+// use XG_GIVEUP_NS, the same by default.  A module compiled with XG_FAIL_WAITS
+// makes those waits unable to succeed, to test the give-up paths: the tile wait
+// polls once, and a TMA staging barrier expects 16 bytes more than its copies
+// deliver (the copies themselves still land, and the CTA drains them before it
+// leaves).
 #ifndef XG_WAIT_NS
 #define XG_WAIT_NS 1000000000ull
 #endif
@@ -389,8 +390,8 @@ __device__ __forceinline__ bool xg_mbar_wait(uint64_t* bar, unsigned parity, uin
 
 // ---------------------------------------------------------------------------
 // Persistent loop kernels: one cooperative launch runs K iterations of a launch
-// group, each CTA walking the tiles blockIdx.x, blockIdx.x + gridDim.x, ... and
-// all CTAs meeting at a grid barrier between iterations.
+// group, each CTA walking the tiles blockIdx.x, blockIdx.x + gridDim.x, ... of
+// every iteration in turn, each tile waiting only for its neighbouring tiles.
 
 // Tile number t of a (ntz, nty, ntx) tiling, numbered like xg_tile_of.
 __device__ __forceinline__ xg_tile xg_tile_at(int64_t t, int64_t Z, int64_t Y, int64_t X, int tz, int ty, int tx,
@@ -407,45 +408,64 @@ __device__ __forceinline__ xg_tile xg_tile_at(int64_t t, int64_t Z, int64_t Y, i
   return T;
 }
 
-// Grid barrier number `gen` (1, 2, ...) of a cooperative launch of `nblocks` CTAs.
-// sync[0] counts arrivals (zero at launch); barrier `gen` is complete when it
-// reaches gen * nblocks.  Thread 0 of each CTA arrives with a release and polls
-// with acquires, so the writes of every CTA before the barrier are visible to
-// every CTA after it.  The poll is bounded: after XG_GIVEUP_NS nanoseconds it sets
-// the error word sync[1] and the CTA leaves (false).
-__device__ __forceinline__ bool xg_grid_sync(unsigned* sync, unsigned nblocks, unsigned gen) {
+// Completion flags of a persistent loop launch: flags[t] counts the iterations
+// tile t has completed (zero at launch).  Iteration k of a tile reads the cells
+// its neighbouring tiles wrote in iteration k - 1 and overwrites the buffer
+// they read in iteration k - 1, so it may start once every tile of its 3 x 3 x 3
+// neighbourhood (tile coordinates, wrapped across the grid when the grid's edges
+// wrap) has completed k iterations -- no grid-wide barrier.  Threads 0..26 each
+// poll one neighbour's flag with acquire loads; the wait gives up after
+// XG_GIVEUP_NS, sets the error word and returns false.  The launch is
+// cooperative, so every CTA whose tiles are waited for is resident.
+__device__ __forceinline__ bool xg_tile_wait(const unsigned* flags, int64_t t, int64_t ntz, int64_t nty,
+                                             int64_t ntx, int wrap, unsigned need, unsigned* err) {
   __shared__ int ok_;
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  if (tid == 0) ok_ = 1;
   __syncthreads();
-  if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
-    const unsigned target = gen * nblocks;
-    __threadfence();
-    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(sync), "r"(1u) : "memory");
-    int ok = 0;
-    const uint64_t t0 = xg_now_ns();
-    for (unsigned i = 0; i < XG_WAIT_POLLS_MAX; ++i) {
-      unsigned v;
-      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(sync) : "memory");
-      if ((int)(v - target) >= 0) {
-        ok = 1;
-        break;
+  if (tid < 27 && tid != 13) {
+    const int64_t n[3] = {ntz, nty, ntx};
+    int64_t c[3] = {t / (ntx * nty), (t / ntx) % nty, t % ntx};
+    const int d[3] = {tid / 9 - 1, (tid / 3) % 3 - 1, tid % 3 - 1};
+    bool skip = false;
+    for (int a = 0; a < 3; ++a) {
+      if (d[a] == 0) continue;
+      if (n[a] == 1) { skip = true; break; }
+      int64_t v = c[a] + d[a];
+      if (v < 0 || v >= n[a]) {
+        if (!wrap) { skip = true; break; }
+        v = (v + n[a]) % n[a];
       }
-      if (xg_now_ns() - t0 >= XG_GIVEUP_NS) break;
+      c[a] = v;
     }
-    if (!ok) atomicExch((int*)(sync + 1), 1);
-    __threadfence();
-    ok_ = ok;
+    if (!skip) {
+      const unsigned* f = flags + (c[0] * nty + c[1]) * ntx + c[2];
+      const uint64_t t0 = xg_now_ns();
+      int ok = 0;
+      for (unsigned i = 0; i < XG_WAIT_POLLS_MAX; ++i) {
+        unsigned v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+        if ((int)(v - need) >= 0) {
+          ok = 1;
+          break;
+        }
+        if (xg_now_ns() - t0 >= XG_GIVEUP_NS) break;
+      }
+      if (!ok) atomicExch(&ok_, 0);
+    }
   }
   __syncthreads();
-  return ok_ != 0;
+  if (ok_) return true;
+  if (tid == 0) atomicExch((int*)err, 1);
+  return false;
 }
 
-// Last arrival of a launch that passed `barriers` grid barriers: the CTA whose
-// arrival completes the count puts it back to zero for the next launch (every
-// CTA has left its last poll by then).
-__device__ __forceinline__ void xg_grid_exit(unsigned* sync, unsigned nblocks, unsigned barriers) {
+// Tile t has completed `done` iterations: every thread's writes, then the flag (release).
+__device__ __forceinline__ void xg_tile_done(unsigned* flags, int64_t t, unsigned done) {
+  __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
-    const unsigned old = atomicAdd(sync, 1u);
-    if (old + 1u == (barriers + 1u) * nblocks) atomicExch(sync, 0u);
+    __threadfence();
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(flags + t), "r"(done) : "memory");
   }
 }
 
@@ -480,6 +500,15 @@ __device__ __forceinline__ __nv_bfloat16 xg_to_store<__nv_bfloat16>(float v) {
 __device__ __forceinline__ float xg_from_store(float v) { return v; }
 __device__ __forceinline__ float xg_from_store(__half v) { return __half2float(v); }
 __device__ __forceinline__ float xg_from_store(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// Four consecutive stored values at element `idx` of a shared-memory array of T,
+// converted to FP32 and multiplied by `scale` (a power of two: exact).
+template <typename T>
+__device__ __forceinline__ float4 xg_ld4_scaled(const void* base, int idx, float scale) {
+  const T* h = (const T*)base + idx;
+  return make_float4(xg_from_store(h[0]) * scale, xg_from_store(h[1]) * scale, xg_from_store(h[2]) * scale,
+                     xg_from_store(h[3]) * scale);
+}
 
 // Largest value over the block (every thread calls it; v >= 0 or NaN) folded
 // into *dst with an integer atomicMax (non-negative floats order like their bits).

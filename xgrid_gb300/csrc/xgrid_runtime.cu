@@ -402,6 +402,72 @@ int xg_mask_tile_local(xg_mask* m, const int32_t* tile, int32_t value, int noff,
   return 0;
 }
 
+int xg_mask_tile_reach(xg_mask* m, const int32_t* tile, int noff, const int32_t* offsets, int overstep, int* ok) {
+  if (!m || !tile || !ok || (noff > 0 && !offsets)) return fail("xg_mask_tile_reach: null argument");
+  const int32_t ext[3] = {tile[0], tile[1], tile[2]};
+  int64_t nt[3], reach[3] = {0, 0, 0};
+  for (int a = 0; a < 3; ++a) {
+    if (ext[a] < 1) return fail("xg_mask_tile_reach: tile extents must be positive");
+    nt[a] = tile_count(m->ext[a], ext[a]);
+    for (int k = 0; k < noff; ++k) reach[a] = std::max<int64_t>(reach[a], std::abs(offsets[3 * k + a]));
+  }
+  // a read may reach the next tile along an axis, never the one after it (the last
+  // tile of an axis absorbs the remainder, so it is at least as long as the others)
+  for (int a = 0; a < 3; ++a)
+    if (nt[a] > 1 && reach[a] > ext[a]) {
+      *ok = 0;
+      return 0;
+    }
+  if (overstep != XG_OVERSTEP_NONE) {  // clamped reads stay put, wrapped reads reach the wrapped neighbour
+    *ok = 1;
+    return 0;
+  }
+  std::string ck("reach");
+  ck.append(reinterpret_cast<const char*>(tile), 3 * sizeof(int32_t));
+  ck.append(reinterpret_cast<const char*>(offsets), (size_t)noff * 3 * sizeof(int32_t));
+  auto hit = m->local_cache.find(ck);
+  if (hit != m->local_cache.end()) {
+    *ok = hit->second;
+    return 0;
+  }
+  // overstep "none" addresses the flattened index: a read past a row or plane end of
+  // the grid lands at the other end of the next row or plane.  Only mask-0 cells
+  // within the reach of the grid's outer faces can do that; check those.
+  int result = 1;
+  const int64_t X = m->ext[2], Y = m->ext[1], Z = m->ext[0];
+  auto tile_of3 = [&](int64_t lin, int64_t* c) {
+    const int64_t x = lin % X, y = (lin / X) % Y, z = lin / (X * Y);
+    c[0] = tile_of(z, ext[0], nt[0]);
+    c[1] = tile_of(y, ext[1], nt[1]);
+    c[2] = tile_of(x, ext[2], nt[2]);
+  };
+  for (int64_t z = 0; z < Z && result; ++z)
+    for (int64_t y = 0; y < Y && result; ++y) {
+      const bool face_zy = z < reach[0] || z >= Z - reach[0] || y < reach[1] || y >= Y - reach[1];
+      for (int64_t x = 0; x < X && result; ++x) {
+        if (!face_zy && x >= reach[2] && x < X - reach[2]) {
+          x = X - reach[2] - 1;  // skip the interior of the row
+          continue;
+        }
+        const int64_t lin = (z * Y + y) * X + x;
+        if (m->host[lin] != 0) continue;
+        int64_t own[3];
+        tile_of3(lin, own);
+        for (int k = 0; k < noff && result; ++k) {
+          const int64_t t = address(m, lin, offsets + 3 * k, overstep);
+          if (t < 0) continue;  // outside the allocation: the kernel reads zero there
+          int64_t c[3];
+          tile_of3(t, c);
+          for (int a = 0; a < 3; ++a)
+            if (std::abs(c[a] - own[a]) > 1) result = 0;
+        }
+      }
+    }
+  m->local_cache.emplace(ck, result);
+  *ok = result;
+  return 0;
+}
+
 int xg_mask_boxes(xg_mask* m, const int32_t* core, const int32_t* halo, int32_t value, const uint8_t** box_zero,
                   const int32_t** off, const int32_t** local, int64_t* ntiles) {
   if (!m || !core || !halo) return fail("xg_mask_boxes: null argument");
@@ -673,19 +739,35 @@ void xg_prof_enable(int on) {
 
 int xg_prof_enabled(void) { return g_prof_on; }
 
+// While `stream` is being captured into a CUDA graph the events become event-record
+// nodes of the graph (cudaEventRecordExternal): every replay of the graph records
+// them again, so xg_prof_read then gives the launch durations of the latest replay.
+static bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &st) == cudaSuccess && st == cudaStreamCaptureStatusActive;
+}
+
+static void prof_record(cudaEvent_t e, cudaStream_t s) {
+  if (capturing(s))
+    cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+  else
+    cudaEventRecord(e, s);
+}
+
 void xg_prof_launch(int group, void* stream) {
   std::lock_guard<std::mutex> lock(g_prof_mu);
   g_launches += 1;
   if (!g_prof_on) return;
+  if (g_prof_on == 2 && !capturing(static_cast<cudaStream_t>(stream))) return;
   ProfRec r{group, pooled_event(), pooled_event()};
-  cudaEventRecord(r.start, static_cast<cudaStream_t>(stream));
+  prof_record(r.start, static_cast<cudaStream_t>(stream));
   g_prof.push_back(r);
 }
 
 void xg_prof_end(int group, void* stream) {
   std::lock_guard<std::mutex> lock(g_prof_mu);
   if (!g_prof_on || g_prof.empty() || g_prof.back().group != group) return;
-  cudaEventRecord(g_prof.back().stop, static_cast<cudaStream_t>(stream));
+  prof_record(g_prof.back().stop, static_cast<cudaStream_t>(stream));
 }
 
 int64_t xg_prof_launches(void) {

@@ -30,7 +30,8 @@ from __future__ import annotations
 
 from . import analysis
 
-BX = 128          # box columns = threads along x; the block has two rows of threads (strips)
+BX = 128          # box columns: 32 lanes x 4 columns per lane
+NW = 8            # warps per CTA, stacked along y; each owns RS rows of the box
 DSCALE = 8        # defect: an input of largest magnitude m is stored as m * 2^s in [2^8, 2^9)
 RSCALE = 14       # residual (fixed over the loop): [2^14, 2^15), below the FP16 maximum
 STORAGE = {"fp32": ("float", 0, "CU_TENSOR_MAP_DATA_TYPE_FLOAT32"),
@@ -72,26 +73,30 @@ class TemporalDefect:
         self.main_offs = target_offsets(self.sweeps[0], self.slot)
         self.sy = max([abs(o[1]) for o in self.main_offs] + [0])
         self.sx = max([abs(o[2]) for o in self.main_offs] + [0])
-        self.usable = self.dim == 2 and all(o[0] == 0 for o in self.main_offs)
+        # the register blocks reach one row and one column beyond themselves
+        self.usable = (self.dim == 2 and all(o[0] == 0 for o in self.main_offs)
+                       and self.sy <= 1 and self.sx <= 1)
 
     # ----------------------------------------------------------- device code
     def _lin(self, sweep, load) -> str:
         code = self.LinearEmitter(self.mx, self.target, load).lin(sweep.stmt.value)
         return "0.0f" if code is None else code
 
-    def _strip_loader(self, buf: str):
-        """Load of the defect at a stencil offset for row i of the thread's strip."""
+    def _reg_loader(self, j: int, used: set):
+        """Load of the defect at a stencil offset for column ``j`` (0..3) of the
+        thread's 4-column block: rows above / at / below come from the register
+        rows ``prev`` / ``cur`` / ``nxt``, columns beyond the block from the
+        neighbouring lanes (``<row>_w``: lane - 1's last column, ``<row>_e``:
+        lane + 1's first column).  ``used`` collects the lane exchanges needed."""
         def load(st):
             oz, oy, ox = analysis.pad3(st.space_offset)
-            cx = "lx" if ox == 0 else f"cx_{'m' if ox < 0 else 'p'}{abs(ox)}"
-            # rows inside the thread's strip need no clamp (decided at compile time once i is unrolled)
-            row = f"((i + ({oy}) >= 0 && i + ({oy}) < RS) ? ly0 + i + ({oy}) : xg_clampi(ly0 + i + ({oy}), 0, BY - 1))"
-            smem = f"{buf}[{row} * BX + {cx}]"
-            if ox == 0 and oy == 0:
-                return "d[i]"
-            if ox == 0:
-                return f"((i + ({oy}) >= 0 && i + ({oy}) < RS) ? d[xg_clampi(i + ({oy}), 0, RS - 1)] : {smem})"
-            return smem
+            row = {-1: "prev", 0: "cur", 1: "nxt"}[oy]
+            jj = j + ox
+            if 0 <= jj <= 3:
+                return f"{row}.{'xyzw'[jj]}"
+            side = "w" if jj < 0 else "e"
+            used.add((row, side))
+            return f"{row}_{side}"
         return load
 
     @staticmethod
@@ -102,11 +107,12 @@ class TemporalDefect:
         return load
 
     def device(self) -> list:
-        n, gid, dt = self.n, self.gid, self.dt
+        n, gid = self.n, self.gid
         main = self.sweeps[0]
-        xs = sorted({o[2] for o in self.main_offs if o[2]})
+        used: set = set()
+        lins = [self._lin(main, self._reg_loader(j, used)) for j in range(4)]
         P = [f"struct xgp_{n}_{gid}_mxt {{",
-             "  CUtensorMap md;  // defect in (storage type), box 128 x BY",
+             "  CUtensorMap md;  // defect in (storage type), box BX x BY",
              "  CUtensorMap mr;  // residual (FP32 on the first launch and in FP32 mode, else storage type)",
              f"  struct xgm_{n}_{gid} k;",
              "  int Y, X, XP, TY, TX, HY, HX, nty, ntx, dep, first, li;",
@@ -120,15 +126,18 @@ class TemporalDefect:
             P += [f"  const int32_t* bo{j};", f"  const int32_t* bl{j};"]
         P.append("};")
         K = [f"template <typename Dt, int RS>",
-             f"__global__ void __launch_bounds__(256, RS <= 8 ? 4 : (RS <= 16 ? 3 : 2)) xgk_{n}_{gid}_mxt(const __grid_constant__ "
+             f"__global__ void __launch_bounds__({NW * 32}, 2) xgk_{n}_{gid}_mxt(const __grid_constant__ "
              f"struct xgp_{n}_{gid}_mxt p) {{",
-             f"  constexpr int BX = {BX}, BY = 2 * RS;",
+             f"  constexpr int BX = {BX}, NW = {NW}, BY = NW * RS;",
              "  constexpr bool scaled = sizeof(Dt) == 2;",
+             "  constexpr unsigned FULL = 0xffffffffu;",
              "  extern __shared__ unsigned char xg_dsm[];",
              "  __shared__ __align__(8) uint64_t xg_bar;",
+             "  __shared__ __align__(16) float xg_ex[2][2][NW][BX];  // [parity][first/last row][warp][column]",
              "  float* sA = (float*)(((uintptr_t)xg_dsm + 1023) & ~(uintptr_t)1023);",
              "  float* sB = sA + BY * BX;",
-             "  const int lx = threadIdx.x, tid = lx + BX * (int)threadIdx.y, ly0 = (int)threadIdx.y * RS;",
+             "  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;",
+             "  const int c0 = 4 * lane, r0 = w * RS;  // the thread's block: columns c0..c0+3, rows r0..r0+RS-1",
              "  const int t = blockIdx.x;",
              "  const int ity = t / p.ntx, itx = t - ity * p.ntx;",
              "  const int by = ity * p.TY - p.HY, bx = itx * p.TX - p.HX;",
@@ -150,83 +159,103 @@ class TemporalDefect:
              "    }",
              "    return;",
              "  }",
-             "  float d[RS], rr[RS];",
+             "  float4 d[RS], rr[RS];",
              "  {",
              f"    const float ir = (scaled && !p.first) ? xg_pow2f(-xg_scale_exp(p.sl[0], {RSCALE})) : 1.f;",
              f"    const float id = (scaled && !p.first) ? xg_pow2f(-xg_scale_exp(p.sl[p.li - 1], {DSCALE})) : 1.f;",
-             "    const Dt* __restrict__ hA = (const Dt*)sA;",
-             "    const Dt* __restrict__ hB = (const Dt*)sB;",
              "#pragma unroll",
              "    for (int i = 0; i < RS; ++i) {",
-             "      const int c = (ly0 + i) * BX + lx;",
-             "      rr[i] = (p.first || !scaled) ? sB[c] : xg_from_store(hB[c]) * ir;",
-             "      d[i] = p.first ? rr[i] : xg_from_store(hA[c]) * id;",
+             "      const int c = (r0 + i) * BX + c0;",
+             "      rr[i] = (p.first || !scaled) ? *(const float4*)(sB + c) : xg_ld4_scaled<Dt>(sB, c, ir);",
+             "      d[i] = p.first ? rr[i] : (scaled ? xg_ld4_scaled<Dt>(sA, c, id) : *(const float4*)(sA + c));",
              "    }",
              "  }",
-             "  __syncthreads();"]
-        for o in xs:
-            nm = f"cx_{'m' if o < 0 else 'p'}{abs(o)}"
-            K.append(f"  const int {nm} = xg_clampi(lx + ({o}), 0, BX - 1);")
-        K += ["  if (p.bzero[t]) {  // no boundary cell in the box: one pass per iteration",
-              "    for (int k = 0; k < p.dep; ++k) {",
-              "      float* __restrict__ cur = (k & 1) ? sB : sA;",
-              "#pragma unroll",
-              "      for (int i = 0; i < RS; ++i) cur[(ly0 + i) * BX + lx] = d[i];",
-              "      __syncthreads();",
-              "      float nd[RS];",
-              "#pragma unroll",
-              f"      for (int i = 0; i < RS; ++i) nd[i] = {self._lin(main, self._strip_loader('cur'))} + rr[i];",
-              "#pragma unroll",
-              "      for (int i = 0; i < RS; ++i) d[i] = nd[i];",
-              "    }",
-              "  } else {  // main sweep on mask-0 cells, boundary phases in program order, then + r",
-              "    unsigned mz = 0;",
-              "    {",
-              "      const int gx = bx + lx;",
-              "#pragma unroll",
-              "      for (int i = 0; i < RS; ++i) {",
-              "        const int gy = by + ly0 + i;",
-              "        if (gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X && p.m0[(int64_t)gy * p.X + gx] == 0) "
-              "mz |= 1u << i;",
+             "  const bool plain = p.bzero[t] != 0;  // no boundary cell in the box",
+             "  unsigned mz = 0;  // boxes with boundary cells: bit 4 i + j set when cell (r0 + i, c0 + j) has mask 0",
+             "  if (!plain) {",
+             "#pragma unroll",
+             "    for (int i = 0; i < RS; ++i) {",
+             "      const int gy = by + r0 + i;",
+             "#pragma unroll",
+             "      for (int j = 0; j < 4; ++j) {",
+             "        const int gx = bx + c0 + j;",
+             "        if (gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X && p.m0[(int64_t)gy * p.X + gx] == 0) "
+             "mz |= 1u << (4 * i + j);",
+             "      }",
+             "    }",
+             "  }",
+             "  __syncthreads();  // the staged boxes are read: sA and sB become scratch",
+             "  for (int k = 0; k < p.dep; ++k) {",
+             "    // rows next to the warp's block: last row of the warp above, first row of the warp below",
+             "    float (*ex)[NW][BX] = xg_ex[k & 1];",
+             "    *(float4*)&ex[0][w][c0] = d[0];",
+             "    *(float4*)&ex[1][w][c0] = d[RS - 1];",
+             "    __syncthreads();",
+             "    const float4 up = w > 0 ? *(const float4*)&ex[1][w - 1][c0] : d[0];",
+             "    const float4 dn = w < NW - 1 ? *(const float4*)&ex[0][w + 1][c0] : d[RS - 1];",
+             "    float4 prev = up;",
+             "#pragma unroll",
+             "    for (int i = 0; i < RS; ++i) {",
+             "      const float4 cur = d[i];",
+             "      const float4 nxt = i + 1 < RS ? d[i + 1 < RS ? i + 1 : i] : dn;"]
+        for row, side in sorted(used):
+            if side == "w":
+                K.append(f"      const float {row}_w = __shfl_up_sync(FULL, {row}.w, 1);")
+            else:
+                K.append(f"      const float {row}_e = __shfl_down_sync(FULL, {row}.x, 1);")
+        K.append("      float4 nv;")
+        for j in range(4):
+            K.append(f"      nv.{'xyzw'[j]} = {lins[j]};")
+        K += ["      if (plain) {",
+              "        d[i] = make_float4(nv.x + rr[i].x, nv.y + rr[i].y, nv.z + rr[i].z, nv.w + rr[i].w);",
+              "      } else {",
+              "        d[i].x = ((mz >> (4 * i)) & 1u) ? nv.x : cur.x;",
+              "        d[i].y = ((mz >> (4 * i + 1)) & 1u) ? nv.y : cur.y;",
+              "        d[i].z = ((mz >> (4 * i + 2)) & 1u) ? nv.z : cur.z;",
+              "        d[i].w = ((mz >> (4 * i + 3)) & 1u) ? nv.w : cur.w;",
               "      }",
+              "      prev = cur;",
               "    }",
-              "    for (int k = 0; k < p.dep; ++k) {",
+              "    if (!plain) {  // boundary phases in program order on the box in shared memory, then + r",
               "#pragma unroll",
-              "      for (int i = 0; i < RS; ++i) sA[(ly0 + i) * BX + lx] = d[i];",
-              "      __syncthreads();",
-              "      float nd[RS];",
-              "#pragma unroll",
-              f"      for (int i = 0; i < RS; ++i) nd[i] = ((mz >> i) & 1u) ? "
-              f"{self._lin(main, self._strip_loader('sA'))} : d[i];",
-              "#pragma unroll",
-              "      for (int i = 0; i < RS; ++i) sB[(ly0 + i) * BX + lx] = nd[i];",
+              "      for (int i = 0; i < RS; ++i) *(float4*)(sB + (r0 + i) * BX + c0) = d[i];",
               "      __syncthreads();"]
         for j in self.bnds:
-            K += [f"      for (int e = p.bo{j}[t] + tid; e < p.bo{j}[t + 1]; e += 2 * BX) {{",
+            K += [f"      for (int e = p.bo{j}[t] + tid; e < p.bo{j}[t + 1]; e += NW * 32) {{",
                   f"        const int c = p.bl{j}[e];",
                   f"        sB[c] = {self._lin(self.sweeps[j], self._box_loader('sB'))};",
                   "      }",
                   "      __syncthreads();"]
         K += ["#pragma unroll",
-              "      for (int i = 0; i < RS; ++i) d[i] = sB[(ly0 + i) * BX + lx] + rr[i];",
+              "      for (int i = 0; i < RS; ++i) {",
+              "        const float4 v = *(const float4*)(sB + (r0 + i) * BX + c0);",
+              "        d[i] = make_float4(v.x + rr[i].x, v.y + rr[i].y, v.z + rr[i].z, v.w + rr[i].w);",
+              "      }",
               "    }",
               "  }",
-              "  // the tile's own cells go back to global memory",
+              "  // the tile's own cells go back to global memory (the tile's columns are whole 4-column blocks)",
               f"  const float os = scaled ? xg_pow2f(xg_scale_exp(p.sl[p.li], {DSCALE})) : 1.f;",
               f"  const float rs = scaled ? xg_pow2f(xg_scale_exp(p.sl[0], {RSCALE})) : 1.f;",
               "  Dt* __restrict__ dout = (Dt*)p.dout;",
               "  Dt* __restrict__ rout = (Dt*)p.rout;",
-              "  const int gx = bx + lx;",
-              "  const bool col = lx >= p.HX && lx < p.HX + p.TX && gx < p.X;",
+              "  const int gx = bx + c0;",
+              "  const bool col = c0 >= p.HX && c0 < p.HX + p.TX && gx < p.X;",
               "  float amax = 0.f;",
               "#pragma unroll",
               "  for (int i = 0; i < RS; ++i) {",
-              "    const int ly = ly0 + i, gy = by + ly;",
+              "    const int ly = r0 + i, gy = by + ly;",
               "    if (col && ly >= p.HY && ly < p.HY + p.TY && gy < p.Y) {",
               "      const int64_t a = (int64_t)gy * p.XP + gx;",
-              "      dout[a] = xg_to_store<Dt>(d[i] * os);",
-              "      if (scaled && rout) rout[a] = xg_to_store<Dt>(rr[i] * rs);",
-              "      amax = fmaxf(amax, fabsf(d[i]));",
+              "      const float v[4] = {d[i].x, d[i].y, d[i].z, d[i].w};",
+              "      const float q[4] = {rr[i].x, rr[i].y, rr[i].z, rr[i].w};",
+              "#pragma unroll",
+              "      for (int j = 0; j < 4; ++j) {",
+              "        if (gx + j < p.X) {",
+              "          dout[a + j] = xg_to_store<Dt>(v[j] * os);",
+              "          if (scaled && rout) rout[a + j] = xg_to_store<Dt>(q[j] * rs);",
+              "          amax = fmaxf(amax, fabsf(v[j]));",
+              "        }",
+              "      }",
               "    }",
               "  }",
               "  if (scaled) xg_block_max_atomic(amax, p.sl + p.li + 1);",
@@ -254,8 +283,8 @@ class TemporalDefect:
         L = [f"static int32_t xg_mxt_{n}[2] = {{{int(cfg.mixed_temporal)}, {int(cfg.mixed_rows)}}};",
              f'extern "C" int xg_mixed_tb_{n}(int depth, int rows) {{',
              "  if (depth < 0 || depth > 16) XG_FAIL(\"temporal blocking: depth %d outside 0..16\", depth);",
-             "  if (rows >= 0 && rows != 8 && rows != 16 && rows != 24) "
-             "XG_FAIL(\"temporal blocking: rows per thread must be 8, 16 or 24, not %d\", rows);",
+             "  if (rows >= 0 && rows != 4 && rows != 8) "
+             "XG_FAIL(\"temporal blocking: rows per warp must be 4 or 8, not %d\", rows);",
              f"  xg_mxt_{n}[0] = depth;",
              f"  if (rows >= 0) xg_mxt_{n}[1] = rows;",
              "  return 0;",
@@ -266,10 +295,10 @@ class TemporalDefect:
              f"  if (g->ndim != 2 || xg_mxt_{n}[0] < 1 || !g->mask) return 0;",
              f"  *T = xg_mxt_{n}[0];",
              f"  *RS = xg_mxt_{n}[1];",
-             "  if (*RS != 8 && *RS != 16 && *RS != 24) return 0;",
+             "  if (*RS != 4 && *RS != 8) return 0;",
              f"  halo[0] = 0; halo[1] = *T * {self.sy}; halo[2] = (*T * {self.sx} + {self.xalign - 1}) / "
              f"{self.xalign} * {self.xalign};",
-             f"  core[0] = 1; core[1] = 2 * *RS - 2 * halo[1]; core[2] = {BX} - 2 * halo[2];",
+             f"  core[0] = 1; core[1] = {NW} * *RS - 2 * halo[1]; core[2] = {BX} - 2 * halo[2];",
              "  if (core[1] < 1 || core[2] < 8) return 0;",
              f"  const int32_t shrink[3] = {{0, {self.sy}, {self.sx}}};"]
         L += arr("mo", mo) + arr("vals", vals) + arr("nof", nof) + arr("offs", offs)
@@ -282,10 +311,10 @@ class TemporalDefect:
               f"static int xgm_{n}_{gid}_go(const struct xgp_{n}_{gid}_mxt& p, int64_t nt, cudaStream_t s) {{",
               "  static int avail = -1;",
               f"  if (avail < 0) XG_TRY(xg_smem_optin(xgk_{n}_{gid}_mxt<{dt}, RS>, &avail));",
-              f"  const size_t smem = (size_t)2 * (2 * RS) * {BX} * sizeof(float) + 1024;",
+              f"  const size_t smem = (size_t)2 * ({NW} * RS) * {BX} * sizeof(float) + 1024;",
               "  if (smem > (size_t)avail) XG_FAIL(\"temporal blocking: %zu bytes of shared memory, %d available\", "
               "smem, avail);",
-              f"  xgk_{n}_{gid}_mxt<{dt}, RS><<<(unsigned)nt, dim3({BX}, 2, 1), smem, s>>>(p);",
+              f"  xgk_{n}_{gid}_mxt<{dt}, RS><<<(unsigned)nt, {NW * 32}, smem, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
               "  return 0;",
               "}",
@@ -300,7 +329,7 @@ class TemporalDefect:
               "  p.TY = core[1]; p.TX = core[2]; p.HY = halo[1]; p.HX = halo[2];",
               "  p.nty = (p.Y + p.TY - 1) / p.TY; p.ntx = (p.X + p.TX - 1) / p.TX;",
               "  p.dep = dep; p.first = first; p.li = li;",
-              "  const int BY = 2 * RS;",
+              f"  const int BY = {NW} * RS;",
               f"  const int es = (int)sizeof({dt});",
               f"  if (!first) XG_TRY(xg_tmap_2d(&p.md, din, {self.cutype}, es, e.x, e.y, A->XP * es, {BX}, BY));",
               f"  if (first || !{int(self.scaled)})",
@@ -320,9 +349,8 @@ class TemporalDefect:
         L += ["  if (nt != (int64_t)p.nty * p.ntx) XG_FAIL(\"box table mismatch\");",
               f"  xg_prof_launch({gid * 64 + 59}, s);",
               "  switch (RS) {",
+              f"    case 4: XG_TRY(xgm_{n}_{gid}_go<4>(p, nt, s)); break;",
               f"    case 8: XG_TRY(xgm_{n}_{gid}_go<8>(p, nt, s)); break;",
-              f"    case 16: XG_TRY(xgm_{n}_{gid}_go<16>(p, nt, s)); break;",
-              f"    case 24: XG_TRY(xgm_{n}_{gid}_go<24>(p, nt, s)); break;",
               "    default: XG_FAIL(\"temporal blocking: %d rows per thread is not compiled\", RS);",
               "  }",
               f"  xg_prof_end({gid * 64 + 59}, s);",

@@ -51,8 +51,8 @@ class NativeKernel:
 
     def set_mixed_temporal(self, depth: int, rows: int | None = None) -> None:
         """Defect iterations per launch of mixed-precision loops (0: one FP32
-        iteration per launch, no shared-memory staging) and rows per thread of
-        the temporally blocked kernel (8, 16 or 24)."""
+        iteration per launch, no shared-memory staging) and rows per warp of
+        the temporally blocked kernel (4 or 8)."""
         fn = getattr(self.lib.dylib, f"xg_mixed_tb_{self.module.name}", None)
         if fn is None:
             self.logger.dead(f"kernel '{self.module.name}' has no temporally blocked mixed-precision loop")
@@ -67,7 +67,7 @@ class NativeKernel:
         runtime.load().xg_graph_clear(self.fn_ptr)
 
     def loop_error(self, clear: bool = False) -> int:
-        """1 when a grid-barrier wait of a persistent loop launch gave up (the
+        """1 when a neighbour-tile wait of a persistent loop launch gave up (the
         results of that call are invalid), else 0; ``clear`` resets the word.
         Synchronises with the device."""
         fn = getattr(self.lib.dylib, f"xg_loop_error_{self.module.name}")
