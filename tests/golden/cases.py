@@ -473,3 +473,52 @@ def depth3():
     for _ in range(6):
         leap(u, 0.1)
     return {"u": levels(u)}
+
+
+# --------------------------------------------- C interop inside grid sweeps
+def _same_type(args):
+    return args[0]
+
+
+@xgrid.external(name="fabs", typecheck_override=_same_type)
+def fabs(x: float) -> float:
+    ...
+
+
+@xgrid.external(name="XG_TWICE", typecheck_override=_same_type)
+def twice(x: float) -> float:
+    ...
+
+
+@xgrid.function()
+def smaller(a: float, b: float) -> float:
+    r = 0.0
+    with xgrid.c():
+        "r = a < b ? a : b;"
+    return r
+
+
+@case
+def c_interop():
+    """Sweeps that call an external C function (``fabs`` from ``math.h``, included
+    by ``import math``), a kernel macro used through an external name, and a
+    helper whose body is inline C; inline C in the kernel body between sweeps."""
+    xgrid.init(cacheroot=CACHEROOT, opt_level=3, precision="double")
+
+    @xgrid.kernel(macro=["#define XG_TWICE(x) (2.0 * (x))"])
+    def dev(u: xgrid.grid[float, 2], w: float) -> None:
+        import math
+        s = w
+        with xgrid.c():
+            "s = s * 0.5;"
+        u[0, 0] = smaller(fabs(u[0, 1] - u[0, -1]), twice(u[1, 0])) + s * u[-1, 0]
+        with xgrid.boundary(1):
+            u[0, 0] = fabs(u[0, 0] - 0.5) * 0.5
+
+    n = 18
+    u = xgrid.Grid((n, n), float)
+    u.now[...] = np.random.default_rng(12).random((n, n))
+    u.boundary[0, :] = u.boundary[-1, :] = u.boundary[:, 0] = u.boundary[:, -1] = 1
+    for w in (0.3, -0.7, 1.1):
+        dev(u, w)
+    return {"u": levels(u)}

@@ -11,6 +11,9 @@ from oracle import xgrid_oracle
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 INDEX = json.load(open(os.path.join(HERE, "golden_index.json")))
+# cases that run C the numpy oracle does not interpret (inline C, C externals,
+# macros): the GPU tests compare those with the reference's recording directly
+REFERENCE_ONLY = {"c_interop"}
 
 
 def same_bits(a: np.ndarray, b: np.ndarray) -> bool:
@@ -26,7 +29,7 @@ def cases(tmp_path_factory):
     return load_cases(xgrid_oracle, str(tmp_path_factory.mktemp("oracle")), "oracle")
 
 
-@pytest.mark.parametrize("name", sorted(INDEX))
+@pytest.mark.parametrize("name", sorted(set(INDEX) - REFERENCE_ONLY))
 def test_oracle_matches_reference(cases, name):
     assert INDEX[name] == "ok"
     out = cases.CASES[name]()

@@ -276,10 +276,11 @@ class CudaGenerator:
             return f"xg_make_{e.operator.type.name}({', '.join(args)})"
         op: Operator = e.operator
         if op.mode == "external":
+            # an external names a C function or macro that the kernel's includes, macros or
+            # the CUDA headers provide; inside a sweep it runs on the device, so it must be
+            # device-callable there (CUDA's math functions are, and so is a macro)
             if op.name in ("tick",):
                 self.logger.dead(f"External operator '{op.name}' has no implementation")
-            if env.device:
-                self.logger.dead(f"External operator '{op.name}' cannot be called inside a grid sweep on the GPU")
             return f"{op.name}({', '.join(args)})"
         return f"{self.function(op)}({', '.join(args)})"
 
@@ -510,6 +511,13 @@ class CudaGenerator:
         src: list[str] = ['#include "xgrid_gen.cuh"']
         for inc in self.op.includes:
             src.append(f'#include "{inc}"')
+        # preprocessor lines of the kernel's macros also precede the device code, so
+        # that sweeps (externals named after a macro) see them; every macro line is
+        # still emitted at the top of the entry's body, where the reference puts it
+        # (xgrid/lang/generator.py:223-224)
+        for m in self.op.macro:
+            if m.lstrip().startswith("#"):
+                src.append(m)
         src.append("")
         fn_protos, fn_defs = self.function_defs()
         src.extend(self.struct_defs())
