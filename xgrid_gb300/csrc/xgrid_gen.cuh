@@ -353,16 +353,18 @@ __device__ __forceinline__ void xg_tma_load_2d(void* dst, const CUtensorMap* map
 // makes those waits unable to succeed, to test the give-up paths: the tile wait
 // polls once, and a TMA staging barrier expects 16 bytes more than its copies
 // deliver (the copies themselves still land, and the CTA drains them before it
-// leaves).
+// leaves; XG_DRAIN_NS bounds that wait).
 #ifndef XG_WAIT_NS
 #define XG_WAIT_NS 1000000000ull
 #endif
 #ifdef XG_FAIL_WAITS
 #define XG_GIVEUP_NS 0ull
 #define XG_TMA_TX_EXTRA 16u
+#define XG_DRAIN_NS 20000000ull  // the copies land in microseconds; their barrier never completes here
 #else
 #define XG_GIVEUP_NS XG_WAIT_NS
 #define XG_TMA_TX_EXTRA 0u
+#define XG_DRAIN_NS XG_WAIT_NS
 #endif
 #define XG_WAIT_POLLS_MAX (1u << 30)  // a second bound that does not depend on the timer
 
