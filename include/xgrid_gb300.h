@@ -79,6 +79,19 @@ typedef int (*xg_entry_fn)(xg_grid* grids, int ngrids, const void* args, size_t 
                            void* ret, size_t nret, void* stream);
 
 /*
+ * Launch hook of a generated module (no counterpart in the reference, which
+ * runs one grid in one process).  A module exports
+ *     int xg_set_hook_<name>(xg_launch_hook_fn fn, void* ctx);
+ * With a hook set, every single-sweep launch first calls fn(ctx, site, grids,
+ * ngrids, stream), site = launch group * 64 + sweep index within the group:
+ * the slab decomposition refreshes the halo rows of the buffers that sweep
+ * reads across slabs there (xgrid_gb300.slab).  A nonzero return fails the
+ * call.  Fused launches, persistent loops and mixed-precision loops call no
+ * hook: callers that set one run the module with fusion off and without them.
+ */
+typedef int (*xg_launch_hook_fn)(void* ctx, int site, xg_grid* grids, int ngrids, void* stream);
+
+/*
  * No-alloc variant of an entry point (no counterpart in the reference).
  * A kernel declared with @xgrid.kernel(noalloc=True) also exports
  *     xg_kernel_<name>_noalloc

@@ -112,9 +112,10 @@ class _Return(Exception):
 class Interpreter:
     """Executes one operator's IR."""
 
-    def __init__(self, defn: ir.Definition, overstep: str) -> None:
+    def __init__(self, defn: ir.Definition, overstep: str, before_sweep=None) -> None:
         self.defn = defn
         self.overstep = overstep
+        self.before_sweep = before_sweep  # callable(stmt, env) run before every grid sweep
 
     # ----------------------------------------------------------- types
     def ctype(self, e) -> str:
@@ -305,6 +306,8 @@ class Interpreter:
         return t
 
     def sweep(self, stmt: ir.Assignment, env):
+        if self.before_sweep is not None:  # e.g. a slab decomposition refreshing halo rows
+            self.before_sweep(stmt, env)
         target: ir.Stencil = stmt.terminal
         g = env[target.variable.name]
         cells = tuple(c.reshape(-1).astype(np.int64) for c in np.indices(g.shape))

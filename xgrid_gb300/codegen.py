@@ -531,6 +531,10 @@ class CudaGenerator:
             src.append("  char xg_empty;")
         src.append("};")
         src.append(f"static int xg_fuse_{name} = {1 if self.cfg.fuse else 0};")
+        # launch hook (slab decomposition): called before every single-sweep launch with the
+        # launch's site (group * 64 + sweep), so that a caller can refresh halo rows first
+        src.append(f"static xg_launch_hook_fn xg_hook_{name} = NULL;")
+        src.append(f"static void* xg_hook_ctx_{name} = NULL;")
         src.append(f"static int64_t xg_mixed_every_{name} = {int(self.cfg.mixed_every)};")
         src.append(f"static int32_t xg_tiling_{name}[{max(self.group_counter[0], 1)}][6] = {{")
         for gi in range(max(self.group_counter[0], 1)):
@@ -555,6 +559,11 @@ class CudaGenerator:
         src.append("  return 0;")
         src.append("}")
         src.append(f'extern "C" int xg_groups_{name}(void) {{ return {self.group_counter[0]}; }}')
+        src.append(f'extern "C" int xg_set_hook_{name}(xg_launch_hook_fn fn, void* ctx) {{')
+        src.append(f"  xg_hook_{name} = fn;")
+        src.append(f"  xg_hook_ctx_{name} = ctx;")
+        src.append("  return 0;")
+        src.append("}")
         src.append(f'extern "C" int xg_get_tiling_{name}(int group, int32_t* cfg) {{')
         src.append(f"  if (group < 0 || group >= {max(self.group_counter[0], 1)}) return -1;")
         src.append(f"  for (int i = 0; i < 6; ++i) cfg[i] = xg_tiling_{name}[group][i];")
@@ -1563,6 +1572,7 @@ class SweepGroupEmitter:
         site = gid * 64 + j
         L += ["  dim3 block(tl[3], tl[4], tl[5]), grid;",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
+              f"  if (xg_hook_{n}) XG_TRY(xg_hook_{n}(xg_hook_ctx_{n}, {site}, G, {len(self.gen.slots)}, s));",
               f"  xg_prof_launch({site}, s);",
               f"  if (xg_small_index(p.Z, p.Y, p.X)) xgk_{n}_{gid}_{tag}<int><<<grid, block, 0, s>>>(p);",
               f"  else xgk_{n}_{gid}_{tag}<int64_t><<<grid, block, 0, s>>>(p);",
@@ -1605,6 +1615,7 @@ class SweepGroupEmitter:
         L += self.fill_params(tag, sweeps, s.slot, s)
         L += [f"  XG_TRY(xg_mask_cells(G[{s.slot}].mask, {s.mask}, &p.cells, &p.ncells));",
               "  if (p.ncells == 0) return 0;",
+              f"  if (xg_hook_{n}) XG_TRY(xg_hook_{n}(xg_hook_ctx_{n}, {gid * 64 + j}, G, {len(self.gen.slots)}, s));",
               "  int64_t nb = (p.ncells + 255) / 256; if (nb > 65535) nb = 65535;",
               f"  xg_prof_launch({gid * 64 + j}, s);",
               f"  xgk_{n}_{gid}_{tag}<<<(unsigned)nb, 256, 0, s>>>(p);",
