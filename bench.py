@@ -667,7 +667,8 @@ def diffusion_section(n: int = 512, steps: int = 500, runs: int = 3, cpu_seconds
             flush.add_(1)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
-        whole.replay()
+        with torch.cuda.stream(s):  # replay() launches on the current stream
+            whole.replay()
         e1.record(s)
         ev.append((e0, e1))
     s.synchronize()

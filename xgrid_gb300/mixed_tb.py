@@ -4,24 +4,18 @@ The defect iteration ``d <- L(d) + r`` of ``xgrid_gb300.mixed`` runs ``T``
 iterations per launch instead of one.  Each CTA owns a tile of ``TY x TX``
 cells and works on a *box*: the tile plus a halo of ``HY = T * sy`` rows and
 ``HX = roundup(T * sx, 16 bytes / element)`` columns per side (``sy, sx``: reach of the loop
-body's main sweep, at most 1).  The box is 128 columns by 64 rows.  The launch is
-persistent: the resident CTAs walk the boxes with two shared-memory stages, and
-for each box
+body's main sweep).  Per launch:
 
-1. one thread has already issued (while the previous box was computed) the TMA
-   loads of the box's ``d`` and ``r`` (``cp.async.bulk.tensor.2d``, completion
-   on the stage's mbarrier); cells outside the grid read as zero; it now issues
-   the next box's loads into the other stage;
-2. every lane takes a block of 4 columns by ``RS`` rows into registers as float4
-   rows (16 warps of 4 rows or 8 warps of 8 rows); per iteration, neighbours in
-   the lane's own columns come from its registers, the columns beyond from the
-   neighbouring lanes (``__shfl_up_sync`` / ``__shfl_down_sync``), the rows
-   beyond the warp's block from the warps above and below through a small
-   double-buffered shared array (one barrier per iteration);
+1. one thread stages the box of ``d`` and of ``r`` into shared memory with two
+   TMA loads (``cp.async.bulk.tensor.2d``, completion on an mbarrier); cells
+   outside the grid read as zero;
+2. every thread takes a column strip of ``RS`` rows of the box into registers
+   (block of 128 x 2 threads, box of 128 x 2*RS cells); vertical neighbours come
+   from the thread's own registers, horizontal and strip-edge neighbours from a
+   shared copy of the current iterate (two buffers, one barrier per iteration);
 3. boxes that contain boundary cells run the loop body's phases in order: the
    main sweep on mask-0 cells, each ``with boundary(k)`` phase on its cells of
-   the box (per-tile lists of box-local indices, in the consumed stage's shared
-   memory), then ``+ r``;
+   the box (per-tile lists of box-local indices), then ``+ r``;
 4. the tile's cells are written back (FP32, or 16-bit with a power-of-two scale
    per field and launch).
 
@@ -36,7 +30,8 @@ from __future__ import annotations
 
 from . import analysis
 
-BX = 128          # box columns: 32 lanes x 4 columns per lane; warps (16 of 4 rows or 8 of 8) stack to 64 rows
+BX = 128          # box columns: 32 lanes x 4 columns per lane
+NW = 8            # warps per CTA, stacked along y; each owns RS rows of the box
 DSCALE = 8        # defect: an input of largest magnitude m is stored as m * 2^s in [2^8, 2^9)
 RSCALE = 14       # residual (fixed over the loop): [2^14, 2^15), below the FP16 maximum
 STORAGE = {"fp32": ("float", 0, "CU_TENSOR_MAP_DATA_TYPE_FLOAT32"),
@@ -131,153 +126,134 @@ class TemporalDefect:
             P += [f"  const int32_t* bo{j};", f"  const int32_t* bl{j};"]
         P.append("};")
         K = [f"template <typename Dt, int RS>",
-             f"__global__ void __launch_bounds__({BX // 4} * (RS == 4 ? 16 : 8), 1) xgk_{n}_{gid}_mxt("
-             f"const __grid_constant__ struct xgp_{n}_{gid}_mxt p) {{",
-             f"  constexpr int BX = {BX}, NW = RS == 4 ? 16 : 8, BY = NW * RS;",
+             f"__global__ void __launch_bounds__({NW * 32}, 2) xgk_{n}_{gid}_mxt(const __grid_constant__ "
+             f"struct xgp_{n}_{gid}_mxt p) {{",
+             f"  constexpr int BX = {BX}, NW = {NW}, BY = NW * RS;",
              "  constexpr bool scaled = sizeof(Dt) == 2;",
              "  constexpr unsigned FULL = 0xffffffffu;",
              "  extern __shared__ unsigned char xg_dsm[];",
-             "  __shared__ __align__(8) uint64_t xg_bar[2];",
+             "  __shared__ __align__(8) uint64_t xg_bar;",
              "  __shared__ __align__(16) float xg_ex[2][2][NW][BX];  // [parity][first/last row][warp][column]",
-             "  // two stages, each the boxes of d and r (FP32-sized: they double as scratch once read)",
-             "  float* const stage0 = (float*)(((uintptr_t)xg_dsm + 1023) & ~(uintptr_t)1023);",
+             "  float* sA = (float*)(((uintptr_t)xg_dsm + 1023) & ~(uintptr_t)1023);",
+             "  float* sB = sA + BY * BX;",
              "  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;",
              "  const int c0 = 4 * lane, r0 = w * RS;  // the thread's block: columns c0..c0+3, rows r0..r0+RS-1",
-             "  const int nt = p.nty * p.ntx;",
-             "  const unsigned tx_bytes = (unsigned)(BY * BX) * ((p.first || !scaled) ? 4u : (unsigned)sizeof(Dt)) + "
-             "(p.first ? 0u : (unsigned)(BY * BX * sizeof(Dt))) + XG_TMA_TX_EXTRA;",
-             "  if (tid == 0) {",
-             "    xg_mbar_init(&xg_bar[0], 1);",
-             "    xg_mbar_init(&xg_bar[1], 1);",
-             "  }",
+             "  const int t = blockIdx.x;",
+             "  const int ity = t / p.ntx, itx = t - ity * p.ntx;",
+             "  const int by = ity * p.TY - p.HY, bx = itx * p.TX - p.HX;",
+             "  // stage the boxes of r and (after the first launch) d with TMA",
+             "  if (tid == 0) xg_mbar_init(&xg_bar, 1);",
              "  __syncthreads();",
-             "  // stage the boxes of r and (after the first launch) d of box `b` into stage `st` with TMA",
-             "  auto issue = [&](int b, int st) {",
-             "    const int iy = b / p.ntx, ix = b - iy * p.ntx;",
-             "    float* sd = stage0 + st * 2 * BY * BX;",
-             "    xg_mbar_expect_tx(&xg_bar[st], tx_bytes);",
-             "    xg_tma_load_2d(sd + BY * BX, &p.mr, ix * p.TX - p.HX, iy * p.TY - p.HY, &xg_bar[st]);",
-             "    if (!p.first) xg_tma_load_2d(sd, &p.md, ix * p.TX - p.HX, iy * p.TY - p.HY, &xg_bar[st]);",
-             "  };",
-             "  if (tid == 0 && (int)blockIdx.x < nt) issue(blockIdx.x, 0);",
-             "  unsigned phase0 = 0u, phase1 = 0u;  // parity of each stage's next completion",
-             "  float amax = 0.f;",
-             f"  const float ir = (scaled && !p.first) ? xg_pow2f(-xg_scale_exp(p.sl[0], {RSCALE})) : 1.f;",
-             f"  const float id = (scaled && !p.first) ? xg_pow2f(-xg_scale_exp(p.sl[p.li - 1], {DSCALE})) : 1.f;",
-             f"  const float os = scaled ? xg_pow2f(xg_scale_exp(p.sl[p.li], {DSCALE})) : 1.f;",
-             f"  const float rs = scaled ? xg_pow2f(xg_scale_exp(p.sl[0], {RSCALE})) : 1.f;",
-             "  int ib = 0;  // boxes done by this CTA",
-             "  for (int t = blockIdx.x; t < nt; t += gridDim.x, ++ib) {",
-             "    const int st = ib & 1, tn = t + (int)gridDim.x;",
-             "    // every thread is done with the other stage (the previous box, its scratch use included)",
-             "    __syncthreads();",
-             "    if (tid == 0 && tn < nt) {",
-             "      asm volatile(\"fence.proxy.async.shared::cta;\" ::: \"memory\");",
-             "      issue(tn, st ^ 1);",
+             "  if (tid == 0) {",
+             "    const unsigned rb = (p.first || !scaled) ? 4u : (unsigned)sizeof(Dt);",
+             "    xg_mbar_expect_tx(&xg_bar, (unsigned)(BY * BX) * (rb + (p.first ? 0u : (unsigned)sizeof(Dt))) + "
+             "XG_TMA_TX_EXTRA);",
+             "    xg_tma_load_2d(sB, &p.mr, bx, by, &xg_bar);",
+             "    if (!p.first) xg_tma_load_2d(sA, &p.md, bx, by, &xg_bar);",
+             "  }",
+             "  const bool landed = xg_mbar_wait(&xg_bar, 0, XG_GIVEUP_NS);",
+             "  if (__syncthreads_or(!landed)) {  // the copy did not complete: report, let it drain, stop",
+             "    if (tid == 0) {",
+             "      atomicExch(p.err, 1);",
+             "      xg_mbar_wait(&xg_bar, 0, XG_WAIT_NS);",
              "    }",
-             "    const unsigned ph = st ? phase1 : phase0;",
-             "    const bool landed = xg_mbar_wait(&xg_bar[st], ph, XG_GIVEUP_NS);",
-             "    if (__syncthreads_or(!landed)) {  // a copy did not complete: report, let the copies drain, stop",
-             "      if (tid == 0) {",
-             "        atomicExch(p.err, 1);",
-             "        xg_mbar_wait(&xg_bar[st], ph, XG_DRAIN_NS);",
-             "        if (tn < nt) xg_mbar_wait(&xg_bar[st ^ 1], st ? phase0 : phase1, XG_DRAIN_NS);",
-             "      }",
-             "      return;",
-             "    }",
-             "    if (st) phase1 ^= 1u; else phase0 ^= 1u;",
-             "    float* const sA = stage0 + st * 2 * BY * BX;  // d box, then scratch",
-             "    float* const sB = sA + BY * BX;                // r box, then scratch",
-             "    const int ity = t / p.ntx, itx = t - ity * p.ntx;",
-             "    const int by = ity * p.TY - p.HY, bx = itx * p.TX - p.HX;",
-             "    float4 d[RS], rr[RS];",
+             "    return;",
+             "  }",
+             "  float4 d[RS], rr[RS];",
+             "  {",
+             f"    const float ir = (scaled && !p.first) ? xg_pow2f(-xg_scale_exp(p.sl[0], {RSCALE})) : 1.f;",
+             f"    const float id = (scaled && !p.first) ? xg_pow2f(-xg_scale_exp(p.sl[p.li - 1], {DSCALE})) : 1.f;",
              "#pragma unroll",
              "    for (int i = 0; i < RS; ++i) {",
              "      const int c = (r0 + i) * BX + c0;",
              "      rr[i] = (p.first || !scaled) ? *(const float4*)(sB + c) : xg_ld4_scaled<Dt>(sB, c, ir);",
              "      d[i] = p.first ? rr[i] : (scaled ? xg_ld4_scaled<Dt>(sA, c, id) : *(const float4*)(sA + c));",
              "    }",
-             "    const bool plain = p.bzero[t] != 0;  // no boundary cell in the box",
-             "    unsigned mz = 0;  // boxes with boundary cells: bit 4 i + j set when cell (r0 + i, c0 + j) has mask 0",
-             "    if (!plain) {",
+             "  }",
+             "  const bool plain = p.bzero[t] != 0;  // no boundary cell in the box",
+             "  unsigned mz = 0;  // boxes with boundary cells: bit 4 i + j set when cell (r0 + i, c0 + j) has mask 0",
+             "  if (!plain) {",
              "#pragma unroll",
-             "      for (int i = 0; i < RS; ++i) {",
-             "        const int gy = by + r0 + i;",
+             "    for (int i = 0; i < RS; ++i) {",
+             "      const int gy = by + r0 + i;",
              "#pragma unroll",
-             "        for (int j = 0; j < 4; ++j) {",
-             "          const int gx = bx + c0 + j;",
-             "          if (gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X && p.m0[(int64_t)gy * p.X + gx] == 0) "
+             "      for (int j = 0; j < 4; ++j) {",
+             "        const int gx = bx + c0 + j;",
+             "        if (gy >= 0 && gy < p.Y && gx >= 0 && gx < p.X && p.m0[(int64_t)gy * p.X + gx] == 0) "
              "mz |= 1u << (4 * i + j);",
-             "        }",
              "      }",
              "    }",
-             "    for (int k = 0; k < p.dep; ++k) {",
-             "      // rows next to the warp's block: last row of the warp above, first row of the warp below",
-             "      float (*ex)[NW][BX] = xg_ex[k & 1];",
-             "      *(float4*)&ex[0][w][c0] = d[0];",
-             "      *(float4*)&ex[1][w][c0] = d[RS - 1];",
-             "      __syncthreads();",
-             "      const float4 up = w > 0 ? *(const float4*)&ex[1][w - 1][c0] : d[0];",
-             "      const float4 dn = w < NW - 1 ? *(const float4*)&ex[0][w + 1][c0] : d[RS - 1];",
-             "      float4 prev = up;",
+             "  }",
+             "  __syncthreads();  // the staged boxes are read: sA and sB become scratch",
+             "  for (int k = 0; k < p.dep; ++k) {",
+             "    // rows next to the warp's block: last row of the warp above, first row of the warp below",
+             "    float (*ex)[NW][BX] = xg_ex[k & 1];",
+             "    *(float4*)&ex[0][w][c0] = d[0];",
+             "    *(float4*)&ex[1][w][c0] = d[RS - 1];",
+             "    __syncthreads();",
+             "    const float4 up = w > 0 ? *(const float4*)&ex[1][w - 1][c0] : d[0];",
+             "    const float4 dn = w < NW - 1 ? *(const float4*)&ex[0][w + 1][c0] : d[RS - 1];",
+             "    float4 prev = up;",
              "#pragma unroll",
-             "      for (int i = 0; i < RS; ++i) {",
-             "        const float4 cur = d[i];",
-             "        const float4 nxt = i + 1 < RS ? d[i + 1 < RS ? i + 1 : i] : dn;"]
+             "    for (int i = 0; i < RS; ++i) {",
+             "      const float4 cur = d[i];",
+             "      const float4 nxt = i + 1 < RS ? d[i + 1 < RS ? i + 1 : i] : dn;"]
         for row, side in sorted(used):
             if side == "w":
-                K.append(f"        const float {row}_w = __shfl_up_sync(FULL, {row}.w, 1);")
+                K.append(f"      const float {row}_w = __shfl_up_sync(FULL, {row}.w, 1);")
             else:
-                K.append(f"        const float {row}_e = __shfl_down_sync(FULL, {row}.x, 1);")
-        K.append("        float4 nv;")
+                K.append(f"      const float {row}_e = __shfl_down_sync(FULL, {row}.x, 1);")
+        K.append("      float4 nv;")
         for j in range(4):
-            K.append(f"        nv.{'xyzw'[j]} = {lins[j]};")
-        K += ["        if (plain) {",
-              "          d[i] = make_float4(nv.x + rr[i].x, nv.y + rr[i].y, nv.z + rr[i].z, nv.w + rr[i].w);",
-              "        } else {",
-              "          d[i].x = ((mz >> (4 * i)) & 1u) ? nv.x : cur.x;",
-              "          d[i].y = ((mz >> (4 * i + 1)) & 1u) ? nv.y : cur.y;",
-              "          d[i].z = ((mz >> (4 * i + 2)) & 1u) ? nv.z : cur.z;",
-              "          d[i].w = ((mz >> (4 * i + 3)) & 1u) ? nv.w : cur.w;",
-              "        }",
-              "        prev = cur;",
+            K.append(f"      nv.{'xyzw'[j]} = {lins[j]};")
+        K += ["      if (plain) {",
+              "        d[i] = make_float4(nv.x + rr[i].x, nv.y + rr[i].y, nv.z + rr[i].z, nv.w + rr[i].w);",
+              "      } else {",
+              "        d[i].x = ((mz >> (4 * i)) & 1u) ? nv.x : cur.x;",
+              "        d[i].y = ((mz >> (4 * i + 1)) & 1u) ? nv.y : cur.y;",
+              "        d[i].z = ((mz >> (4 * i + 2)) & 1u) ? nv.z : cur.z;",
+              "        d[i].w = ((mz >> (4 * i + 3)) & 1u) ? nv.w : cur.w;",
               "      }",
-              "      if (!plain) {  // boundary phases in program order on the box in shared memory, then + r",
+              "      prev = cur;",
+              "    }",
+              "    if (!plain) {  // boundary phases in program order on the box in shared memory, then + r",
               "#pragma unroll",
-              "        for (int i = 0; i < RS; ++i) *(float4*)(sB + (r0 + i) * BX + c0) = d[i];",
-              "        __syncthreads();"]
+              "      for (int i = 0; i < RS; ++i) *(float4*)(sB + (r0 + i) * BX + c0) = d[i];",
+              "      __syncthreads();"]
         for j in self.bnds:
-            K += [f"        for (int e = p.bo{j}[t] + tid; e < p.bo{j}[t + 1]; e += NW * 32) {{",
-                  f"          const int c = p.bl{j}[e];",
-                  f"          sB[c] = {self._lin(self.sweeps[j], self._box_loader('sB'))};",
-                  "        }",
-                  "        __syncthreads();"]
+            K += [f"      for (int e = p.bo{j}[t] + tid; e < p.bo{j}[t + 1]; e += NW * 32) {{",
+                  f"        const int c = p.bl{j}[e];",
+                  f"        sB[c] = {self._lin(self.sweeps[j], self._box_loader('sB'))};",
+                  "      }",
+                  "      __syncthreads();"]
         K += ["#pragma unroll",
-              "        for (int i = 0; i < RS; ++i) {",
-              "          const float4 v = *(const float4*)(sB + (r0 + i) * BX + c0);",
-              "          d[i] = make_float4(v.x + rr[i].x, v.y + rr[i].y, v.z + rr[i].z, v.w + rr[i].w);",
-              "        }",
+              "      for (int i = 0; i < RS; ++i) {",
+              "        const float4 v = *(const float4*)(sB + (r0 + i) * BX + c0);",
+              "        d[i] = make_float4(v.x + rr[i].x, v.y + rr[i].y, v.z + rr[i].z, v.w + rr[i].w);",
               "      }",
               "    }",
-              "    // the tile's own cells go back to global memory (the tile's columns are whole 4-column blocks)",
-              "    Dt* __restrict__ dout = (Dt*)p.dout;",
-              "    Dt* __restrict__ rout = (Dt*)p.rout;",
-              "    const int gx = bx + c0;",
-              "    const bool col = c0 >= p.HX && c0 < p.HX + p.TX && gx < p.X;",
+              "  }",
+              "  // the tile's own cells go back to global memory (the tile's columns are whole 4-column blocks)",
+              f"  const float os = scaled ? xg_pow2f(xg_scale_exp(p.sl[p.li], {DSCALE})) : 1.f;",
+              f"  const float rs = scaled ? xg_pow2f(xg_scale_exp(p.sl[0], {RSCALE})) : 1.f;",
+              "  Dt* __restrict__ dout = (Dt*)p.dout;",
+              "  Dt* __restrict__ rout = (Dt*)p.rout;",
+              "  const int gx = bx + c0;",
+              "  const bool col = c0 >= p.HX && c0 < p.HX + p.TX && gx < p.X;",
+              "  float amax = 0.f;",
               "#pragma unroll",
-              "    for (int i = 0; i < RS; ++i) {",
-              "      const int ly = r0 + i, gy = by + ly;",
-              "      if (col && ly >= p.HY && ly < p.HY + p.TY && gy < p.Y) {",
-              "        const int64_t a = (int64_t)gy * p.XP + gx;",
-              "        const float v[4] = {d[i].x, d[i].y, d[i].z, d[i].w};",
-              "        const float q[4] = {rr[i].x, rr[i].y, rr[i].z, rr[i].w};",
+              "  for (int i = 0; i < RS; ++i) {",
+              "    const int ly = r0 + i, gy = by + ly;",
+              "    if (col && ly >= p.HY && ly < p.HY + p.TY && gy < p.Y) {",
+              "      const int64_t a = (int64_t)gy * p.XP + gx;",
+              "      const float v[4] = {d[i].x, d[i].y, d[i].z, d[i].w};",
+              "      const float q[4] = {rr[i].x, rr[i].y, rr[i].z, rr[i].w};",
               "#pragma unroll",
-              "        for (int j = 0; j < 4; ++j) {",
-              "          if (gx + j < p.X) {",
-              "            dout[a + j] = xg_to_store<Dt>(v[j] * os);",
-              "            if (scaled && rout) rout[a + j] = xg_to_store<Dt>(q[j] * rs);",
-              "            amax = fmaxf(amax, fabsf(v[j]));",
-              "          }",
+              "      for (int j = 0; j < 4; ++j) {",
+              "        if (gx + j < p.X) {",
+              "          dout[a + j] = xg_to_store<Dt>(v[j] * os);",
+              "          if (scaled && rout) rout[a + j] = xg_to_store<Dt>(q[j] * rs);",
+              "          amax = fmaxf(amax, fabsf(v[j]));",
               "        }",
               "      }",
               "    }",
@@ -322,7 +298,7 @@ class TemporalDefect:
              "  if (*RS != 4 && *RS != 8) return 0;",
              f"  halo[0] = 0; halo[1] = *T * {self.sy}; halo[2] = (*T * {self.sx} + {self.xalign - 1}) / "
              f"{self.xalign} * {self.xalign};",
-             f"  core[0] = 1; core[1] = (*RS == 4 ? 16 : 8) * *RS - 2 * halo[1]; core[2] = {BX} - 2 * halo[2];",
+             f"  core[0] = 1; core[1] = {NW} * *RS - 2 * halo[1]; core[2] = {BX} - 2 * halo[2];",
              "  if (core[1] < 1 || core[2] < 8) return 0;",
              f"  const int32_t shrink[3] = {{0, {self.sy}, {self.sx}}};"]
         L += arr("mo", mo) + arr("vals", vals) + arr("nof", nof) + arr("offs", offs)
@@ -333,26 +309,12 @@ class TemporalDefect:
               "}",
               f"template <int RS>",
               f"static int xgm_{n}_{gid}_go(const struct xgp_{n}_{gid}_mxt& p, int64_t nt, cudaStream_t s) {{",
-              "  // persistent: as many CTAs as are resident (at most one per box), each walking its boxes with",
-              "  // the next box's TMA copies in flight while it computes the current one",
-              "  constexpr int NW = RS == 4 ? 16 : 8;",
-              "  static int avail = -1, sms = 0;",
+              "  static int avail = -1;",
               f"  if (avail < 0) XG_TRY(xg_smem_optin(xgk_{n}_{gid}_mxt<{dt}, RS>, &avail));",
-              "  if (sms == 0) {",
-              "    int dev = 0;",
-              "    XG_CUDA(cudaGetDevice(&dev));",
-              "    XG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));",
-              "  }",
-              f"  const size_t smem = (size_t)2 * 2 * (NW * RS) * {BX} * sizeof(float) + 1024;",
+              f"  const size_t smem = (size_t)2 * ({NW} * RS) * {BX} * sizeof(float) + 1024;",
               "  if (smem > (size_t)avail) XG_FAIL(\"temporal blocking: %zu bytes of shared memory, %d available\", "
               "smem, avail);",
-              "  int per_sm = 0;",
-              f"  XG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xgk_{n}_{gid}_mxt<{dt}, RS>, NW * 32, "
-              "smem));",
-              "  if (per_sm < 1) XG_FAIL(\"temporal blocking: the defect kernel does not fit on an SM\");",
-              "  const int64_t resident = (int64_t)per_sm * sms;",
-              "  const unsigned nb = (unsigned)(nt < resident ? nt : resident);",
-              f"  xgk_{n}_{gid}_mxt<{dt}, RS><<<nb, NW * 32, smem, s>>>(p);",
+              f"  xgk_{n}_{gid}_mxt<{dt}, RS><<<(unsigned)nt, {NW * 32}, smem, s>>>(p);",
               "  XG_CUDA(cudaGetLastError());",
               "  return 0;",
               "}",
@@ -367,7 +329,7 @@ class TemporalDefect:
               "  p.TY = core[1]; p.TX = core[2]; p.HY = halo[1]; p.HX = halo[2];",
               "  p.nty = (p.Y + p.TY - 1) / p.TY; p.ntx = (p.X + p.TX - 1) / p.TX;",
               "  p.dep = dep; p.first = first; p.li = li;",
-              "  const int BY = (RS == 4 ? 16 : 8) * RS;",
+              f"  const int BY = {NW} * RS;",
               f"  const int es = (int)sizeof({dt});",
               f"  if (!first) XG_TRY(xg_tmap_2d(&p.md, din, {self.cutype}, es, e.x, e.y, A->XP * es, {BX}, BY));",
               f"  if (first || !{int(self.scaled)})",
