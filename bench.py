@@ -79,7 +79,7 @@ def parse_args():
     ap.add_argument("--mixed-n", type=int, default=4097)
     ap.add_argument("--mixed-steps", type=int, default=500)
     ap.add_argument("--no-mixed", action="store_true")
-    ap.add_argument("--mixed-temporal", type=int, default=4,
+    ap.add_argument("--mixed-temporal", type=int, default=8,
                     help="defect iterations per launch of the mixed-precision loop (0: one per launch)")
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--adjoint-n", type=int, default=256)

@@ -47,6 +47,11 @@ OVERSTEP = {"none": "XG_OVERSTEP_NONE", "limit": "XG_OVERSTEP_LIMIT", "wrap": "X
 ZWALK_PLANES = 4
 ZWALK_BLOCKS = 4
 
+# staged z-walk of mask-free 3-D sweeps: (z, y, x) tile, thread rows, planes prefetched
+ZSTAGE_TILE = (32, 16, 64)
+ZSTAGE_BY = 4
+ZSTAGE_AHEAD = 2
+
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
 DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 64, 32, 32, 8, 1), 3: (64, 4, 64, 64, 4, 1)}
 
@@ -531,6 +536,7 @@ class CudaGenerator:
             src.append("  char xg_empty;")
         src.append("};")
         src.append(f"static int xg_fuse_{name} = {1 if self.cfg.fuse else 0};")
+        src.append(f"static int xg_zstage_{name} = 1;  // staged z-walk of mask-free 3-D sweeps (0: register z-walk)")
         # launch hook (slab decomposition): called before every single-sweep launch with the
         # launch's site (group * 64 + sweep), so that a caller can refresh halo rows first
         src.append(f"static xg_launch_hook_fn xg_hook_{name} = NULL;")
@@ -559,6 +565,7 @@ class CudaGenerator:
         src.append("  return 0;")
         src.append("}")
         src.append(f'extern "C" int xg_groups_{name}(void) {{ return {self.group_counter[0]}; }}')
+        src.append(f'extern "C" int xg_zstage_set_{name}(int on) {{ xg_zstage_{name} = on; return 0; }}')
         src.append(f'extern "C" int xg_set_hook_{name}(xg_launch_hook_fn fn, void* ctx) {{')
         src.append(f"  xg_hook_{name} = fn;")
         src.append(f"  xg_hook_ctx_{name} = ctx;")
@@ -1549,6 +1556,114 @@ class SweepGroupEmitter:
                              f"has no scratch buffer\");")
         return lines
 
+    def zstage_buffers(self, j: int):
+        """Buffers a staged z-walk of sweep ``j`` streams through shared memory, or
+        None when the sweep does not qualify: a z-walk sweep (7-point style, edges
+        wrapped or clamped), explicit, every load within one cell in y and x, every
+        loaded buffer of one element type."""
+        s = self.g.sweeps[j]
+        if s.implicit or not self.zmarch_ok([j], []):
+            return None
+        bufs = []
+        for _, ld in s.loads:
+            if abs(ld.offset[1]) > 1 or abs(ld.offset[2]) > 1:
+                return None
+            b = (ld.slot, ld.level, ld.version)
+            if b not in bufs:
+                bufs.append(b)
+        if len({self.elem(b[0]) for b in bufs}) != 1 or self.elem(bufs[0][0]) not in ("float", "double"):
+            return None
+        return bufs
+
+    def zstage_kernel(self, tag: str, j: int, bufs: list) -> str:
+        """Staged z-walk: each CTA owns a (ty, tx) column block of a z chunk and
+        streams the planes z0-1 .. z1 of every read buffer, block plus a one-cell
+        halo, through a ring of shared-memory slots with cp.async (``ZSTAGE_AHEAD``
+        planes beyond the next one in flight); plane z reads its horizontal
+        neighbours and the planes above and below from the ring.  Same arithmetic
+        per cell as the other paths."""
+        n, gid = self.name, self.gid
+        s = self.g.sweeps[j]
+        T = self.elem(bufs[0][0])
+        tz, ty, tx = ZSTAGE_TILE
+        dst = self.bname((s.slot, s.level, s.write_version))
+        nb = len(bufs)
+        names, local = {}, {}
+        pre = []
+        for st, ld in s.loads:
+            if ld not in local:
+                vn = f"l{len(local)}"
+                local[ld] = vn
+                b = bufs.index((ld.slot, ld.level, ld.version))
+                oz, oy, ox = ld.offset
+                slot = "pl_c" if oz == 0 else ("pl_m" if oz < 0 else "pl_p")
+                pre.append(f"        const {T} {vn} = {slot}[{b} * PL + (r + ({oy})) * PX + (c + ({ox}))];")
+            names[id(st)] = local[ld]
+        env = SweepEnv(self.gen, self.hoist_map, names, self.div_map, self.mul_map)
+        val = self.gen.expr(s.stmt.value, env)
+        K = [f"template <typename I> __global__ void __launch_bounds__({tx * ZSTAGE_BY}, 3) "
+             f"xgk_{n}_{gid}_{tag}_zs(const __grid_constant__ struct xgp_{n}_{gid}_{tag} p) {{",
+             f"  constexpr int TZ = {tz}, TY = {ty}, TX = {tx}, BY = {ZSTAGE_BY}, RY = TY / BY, D = {ZSTAGE_AHEAD};",
+             "  constexpr int PX = TX + 2, PY = TY + 2, PL = PY * PX, R = D + 3, NT = TX * BY;",
+             f"  constexpr int NB = {nb}, KE = (PL + NT - 1) / NT;",
+             f"  extern __shared__ __align__(16) unsigned char xg_zs_raw[];",
+             f"  {T}* const ring = ({T}*)xg_zs_raw;  // [R][NB][PL]",
+             "  const int tid = threadIdx.x + TX * threadIdx.y;",
+             "  const int ntx = (int)((p.X + TX - 1) / TX), nty = (int)((p.Y + TY - 1) / TY);",
+             "  const int ix = blockIdx.x % ntx, iy = (blockIdx.x / ntx) % nty, iz = blockIdx.x / (ntx * nty);",
+             "  const int x0 = ix * TX, y0 = iy * TY, z0 = iz * TZ;",
+             "  const int z1 = z0 + TZ < (int)p.Z ? z0 + TZ : (int)p.Z;",
+             "  const I sy = (I)p.X, sz = (I)(p.X * p.Y);",
+             "  // this thread's staging elements: their (wrapped or clamped) offsets in a plane",
+             "  I goff[KE];",
+             "#pragma unroll",
+             "  for (int k = 0; k < KE; ++k) {",
+             "    const int e = tid + k * NT;",
+             "    const int ey = (e < PL ? e / PX : 0) - 1 + y0, ex = (e < PL ? e % PX : 0) - 1 + x0;",
+             "    goff[k] = (I)xg_axis(xg_overstep, ey, (int)p.Y) * sy + (I)xg_axis(xg_overstep, ex, (int)p.X);",
+             "  }"]
+        srcs = ", ".join(f"p.{self.bname(b)}" for b in bufs)
+        K += [f"  const {T}* const src[NB] = {{{srcs}}};",
+              "  auto stage = [&](int q) {  // plane q into its ring slot (no copies for q beyond the chunk)",
+              "    if (q <= z1) {",
+              "      const I zb = (I)xg_axis(xg_overstep, q, (int)p.Z) * sz;",
+              f"      {T}* const slot = ring + ((q - z0 + 1) % R) * NB * PL;",
+              "#pragma unroll",
+              "      for (int b = 0; b < NB; ++b)",
+              "#pragma unroll",
+              "        for (int k = 0; k < KE; ++k) {",
+              "          const int e = tid + k * NT;",
+              "          if (e < PL) xg_cp_async(slot + b * PL + e, src[b] + zb + goff[k]);",
+              "        }",
+              "    }",
+              "    xg_cp_async_commit();",
+              "  };",
+              "#pragma unroll",
+              "  for (int q = 0; q < R - 1; ++q) stage(z0 - 1 + q);",
+              f"  {T}* __restrict__ out = p.{dst};",
+              "  for (int z = z0; z < z1; ++z) {",
+              "    stage(z + D + 1);  // into the slot plane z - 2 used (freed by the barrier below)",
+              "    xg_cp_async_wait_group<D>();  // planes up to z + 1 have landed",
+              "    __syncthreads();",
+              f"    const {T}* const pl_m = ring + ((z - z0) % R) * NB * PL;      // plane z - 1",
+              f"    const {T}* const pl_c = ring + ((z - z0 + 1) % R) * NB * PL;  // plane z",
+              f"    const {T}* const pl_p = ring + ((z - z0 + 2) % R) * NB * PL;  // plane z + 1",
+              "    (void)pl_m; (void)pl_p;",
+              "    const int c = threadIdx.x + 1, x = x0 + (int)threadIdx.x;",
+              "#pragma unroll",
+              "    for (int i = 0; i < RY; ++i) {",
+              "      const int r = threadIdx.y + i * BY + 1, y = y0 + r - 1;",
+              "      if (x < (int)p.X && y < (int)p.Y) {"]
+        K += pre
+        K += [f"        out[(I)z * sz + (I)y * sy + (I)x] = {val};",
+              "      }",
+              "    }",
+              "    __syncthreads();  // the slot of plane z - 1 is free for plane z + D + 2",
+              "  }",
+              "  xg_cp_async_wait_all();",
+              "}"]
+        return "\n".join(K)
+
     def emit_main_single(self, j: int, s) -> None:
         n, gid = self.name, self.gid
         tag = f"s{j}"
@@ -1557,6 +1672,9 @@ class SweepGroupEmitter:
         self.gen.device_chunks.append(self.params_struct(tag, sweeps, extra))
         implicit_scatter = s.implicit and any(s.store_offset)
         self.gen.device_chunks.append(self.main_kernel(tag, [j], []))
+        zbufs = self.zstage_buffers(j)
+        if zbufs:
+            self.gen.device_chunks.append(self.zstage_kernel(tag, j, zbufs))
         L = [f"static int xgl_{n}_{gid}_{tag}(xg_grid* G, const struct xgh_{n}_{gid}* h, cudaStream_t s) {{"]
         L += self.check_levels(sweeps, s)
         L += self.fill_params(tag, sweeps, s.slot, s)
@@ -1570,6 +1688,35 @@ class SweepGroupEmitter:
             L.append(f"  XG_CUDA(cudaMemcpyAsync(p.{dst}, p.{src}, (size_t)(p.e{s.slot}[0] * p.e{s.slot}[1] * "
                      f"p.e{s.slot}[2]) * sizeof(*p.{dst}), cudaMemcpyDeviceToDevice, s));")
         site = gid * 64 + j
+        if zbufs:
+            tz, ty, tx = ZSTAGE_TILE
+            T = self.elem(zbufs[0][0])
+            smem = (ZSTAGE_AHEAD + 3) * len(zbufs) * (ty + 2) * (tx + 2)
+            # a grid without boundary cells takes the staged z-walk (every tile mask-free)
+            L += [f"  if (p.same && xg_zstage_{n}) {{",
+                  "    int64_t nz = 0;",
+                  f"    XG_TRY(xg_mask_nonzero(G[{s.slot}].mask, &nz));",
+                  "    if (nz == 0) {",
+                  f"      const size_t smem = (size_t){smem} * sizeof({T});",
+                  "      static int avail32 = -1, avail64 = -1;",
+                  "      const bool small = xg_small_index(p.Z, p.Y, p.X);",
+                  f"      if (small && avail32 < 0) XG_TRY(xg_smem_optin(xgk_{n}_{gid}_{tag}_zs<int>, &avail32));",
+                  f"      if (!small && avail64 < 0) XG_TRY(xg_smem_optin(xgk_{n}_{gid}_{tag}_zs<int64_t>, &avail64));",
+                  "      if (smem <= (size_t)(small ? avail32 : avail64)) {",
+                  f"        const int64_t nt = ((p.X + {tx - 1}) / {tx}) * ((p.Y + {ty - 1}) / {ty}) * "
+                  f"((p.Z + {tz - 1}) / {tz});",
+                  "        if (nt <= 0x7fffffffLL) {",
+                  f"          if (xg_hook_{n}) XG_TRY(xg_hook_{n}(xg_hook_ctx_{n}, {site}, G, {len(self.gen.slots)}, s));",
+                  f"          xg_prof_launch({site}, s);",
+                  f"          if (small) xgk_{n}_{gid}_{tag}_zs<int><<<(unsigned)nt, dim3({tx}, {ZSTAGE_BY}), smem, s>>>(p);",
+                  f"          else xgk_{n}_{gid}_{tag}_zs<int64_t><<<(unsigned)nt, dim3({tx}, {ZSTAGE_BY}), smem, s>>>(p);",
+                  "          XG_CUDA(cudaGetLastError());",
+                  f"          xg_prof_end({site}, s);",
+                  "          return 0;",
+                  "        }",
+                  "      }",
+                  "    }",
+                  "  }"]
         L += ["  dim3 block(tl[3], tl[4], tl[5]), grid;",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
               f"  if (xg_hook_{n}) XG_TRY(xg_hook_{n}(xg_hook_ctx_{n}, {site}, G, {len(self.gen.slots)}, s));",

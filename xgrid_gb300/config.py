@@ -24,8 +24,9 @@ Backend options (new keywords, all optional):
   ``"fp16"`` and ``"bf16"`` store the defect and the residual between launches
   in 16 bits with a power-of-two scale per field.
 * ``mixed_temporal``: defect iterations per launch of the temporally blocked
-  defect kernel (TMA-staged tile + halo in shared memory); 0 runs one iteration
-  per launch without shared-memory staging (FP32 storage).
+  defect kernel (TMA-staged tile + halo in shared memory; default 8, the fastest
+  of 4/6/8 measured on a GB300 at 4097^2); 0 runs one iteration per launch
+  without shared-memory staging (FP32 storage).
 * ``mixed_rows``: rows per warp of that kernel (4 or 8; the box is 128 columns
   by eight times this many rows, halo included).
 * ``int_adds``: every n-th FP64 addition or subtraction of a sweep runs as an
@@ -82,7 +83,7 @@ class Configuration:
     divisor: bool = True
     mixed_every: int = 0
     autotune: bool = True
-    mixed_temporal: int = 4
+    mixed_temporal: int = 8
     mixed_rows: int = 8
     int_adds: int = 0
     persistent: bool = False
@@ -119,7 +120,7 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
          opt_level: Literal[0, 1, 2, 3] = 2, precision: Literal["float", "double"] = "float",
          exact: bool = True, mixed: Optional[str] = None, graph: bool = True,
          fuse: bool = True, divisor: bool = True, mixed_every: int = 0, autotune: bool = True,
-         mixed_temporal: int = 4, mixed_rows: int = 8, int_adds: int = 0, persistent: bool = False,
+         mixed_temporal: int = 8, mixed_rows: int = 8, int_adds: int = 0, persistent: bool = False,
          fail_waits: bool = False) -> None:
     """Set the global configuration (same keywords as the reference plus GPU options)."""
     global _config

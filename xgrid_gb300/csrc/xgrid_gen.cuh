@@ -655,3 +655,10 @@ __device__ __forceinline__ void xg_cp_async(T* dst, const T* src) {
 }
 
 __device__ __forceinline__ void xg_cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Close the group of this thread's cp.async copies issued since the last commit (an empty
+// group is legal), and wait until at most N of its groups are still in flight.
+__device__ __forceinline__ void xg_cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void xg_cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}

@@ -61,6 +61,14 @@ class NativeKernel:
             self.logger.dead(runtime.last_error())
         runtime.load().xg_graph_clear(self.fn_ptr)
 
+    def set_zstage(self, on: bool) -> None:
+        """Staged z-walk of mask-free 3-D sweeps (planes streamed through shared
+        memory, the default) or the register z-walk (horizontal neighbours through L1)."""
+        fn = getattr(self.lib.dylib, f"xg_zstage_set_{self.module.name}")
+        fn.restype = ctypes.c_int
+        fn(ctypes.c_int(1 if on else 0))
+        runtime.load().xg_graph_clear(self.fn_ptr)
+
     def set_mixed_every(self, every: int) -> None:
         """Iterations between FP64 corrections of mixed-precision loops (0 = once per loop)."""
         self.mixed_fn(int(every))
