@@ -53,24 +53,51 @@ def test_3d_sweeps_match_the_oracle(cacheroot, overstep, precision, masked):
     assert gpu.tobytes() == ref.tobytes()
 
 
+def vardiff_plain(u: xgrid.grid[float, 3], k: xgrid.grid[float, 3], dt: float) -> None:
+    # one sweep (no boundary phase), so every call launches the single-sweep path
+    u[0, 0, 0] = u[0, 0, 0] + dt * ((k[0, 0, 0] + k[1, 0, 0]) * (u[1, 0, 0] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[-1, 0, 0]) * (u[-1, 0, 0] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[0, 1, 0]) * (u[0, 1, 0] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[0, -1, 0]) * (u[0, -1, 0] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[0, 0, 1]) * (u[0, 0, 1] - u[0, 0, 0]) +
+                                    (k[0, 0, 0] + k[0, 0, -1]) * (u[0, 0, -1] - u[0, 0, 0]))
+
+
 @pytest.mark.parametrize("overstep", ["wrap", "limit"])
 @pytest.mark.parametrize("precision", ["double", "float"])
 def test_staged_and_register_zwalk_agree(cacheroot, overstep, precision):
     """Mask-free 3-D grids take the staged z-walk (planes streamed through shared
-    memory); the register z-walk computes the same bits.  Extents are not
-    multiples of the staged tile (32 x 16 x 64) and span several tiles."""
+    memory); the register z-walk computes the same bits, and both equal the
+    oracle.  Extents are not multiples of the staged tile (32 x 16 x 64) and span
+    several tiles; the module's count of staged launches shows which path ran."""
     xgrid.init(precision=precision, cacheroot=cacheroot, opt_level=3, overstep=overstep)
     shape = (70, 35, 131)
+    rng = np.random.default_rng(5)
+    u0, k0 = rng.random(shape), rng.uniform(0.01, 0.1, shape)
     out = []
     for staged in (True, False):
-        k = Operator(vardiff, "kernel", f"vardiff_zs_{overstep}_{precision}_{int(staged)}")
-        rng = np.random.default_rng(5)
+        k = Operator(vardiff_plain, "kernel", f"vardiff_zs_{overstep}_{precision}_{int(staged)}")
         u, kk = xgrid.Grid(shape, float), xgrid.Grid(shape, float)
-        u.now[...] = rng.random(shape)
-        kk.now[...] = rng.uniform(0.01, 0.1, shape)
+        u.now[...] = u0
+        kk._extend_time(2)
+        for lv in kk._data:
+            lv[...] = k0
         k(u, kk, 0.05)  # compiles
         k.native.set_zstage(staged)
+        before = k.native.zstage_launches()
         for _ in range(3):
             k(u, kk, 0.05)
+        assert (k.native.zstage_launches() > before) == staged
         out.append(u.read(0))
+    xgrid_oracle.init(precision=precision, cacheroot=cacheroot, opt_level=3, overstep=overstep)
+    ko = xgrid_oracle.kernel()(vardiff_plain)
+    u, kk = xgrid_oracle.Grid(shape, float), xgrid_oracle.Grid(shape, float)
+    u.now[...] = u0
+    kk._extend_time(2)
+    for lv in kk._data:
+        lv[...] = k0
+    for _ in range(4):
+        ko(u, kk, 0.05)
+    ref = np.array(u.now)
     assert out[0].tobytes() == out[1].tobytes()
+    assert out[0].tobytes() == ref.tobytes()

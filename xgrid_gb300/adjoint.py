@@ -258,7 +258,7 @@ class AdjointGenerator:
         allofs = [tuple(o for o in off) for off in lam_offsets] + [k[2] for k in loads_needed]
         lo = [min([0] + [o[a_] for o in allofs]) for a_ in range(3)]
         hi = [max([0] + [o[a_] for o in allofs]) for a_ in range(3)]
-        from .codegen import CELL_LOOP, TILE_PROLOGUE
+        from .codegen import CELL_LOOP, TILE_PROLOGUE, zstage_frame, zstage_launch
 
         from .codegen import SweepGroupEmitter
         axis_name = SweepGroupEmitter.axis_name
@@ -299,14 +299,20 @@ class AdjointGenerator:
                     out.append(f"      if (p.g{slot}) p.g{slot}[c] = p.g{slot}[c] + ({total});")
             return out
 
-        def outputs(idx: str, ind: str) -> list:
+        def totals() -> list:
+            # (slot, adjoint value of the cell) for lam and every coefficient gradient
             out = []
             for slot in slots_used:
                 acc = []
                 for off, d in terms.get(slot, []):
                     lam = names[("lam", tuple(-o for o in off))]
                     acc.append(f"({lam} * {self.emit_sym(d, loadname)})")
-                total = " + ".join(acc) if acc else f"(({T})0)"
+                out.append((slot, " + ".join(acc) if acc else f"(({T})0)"))
+            return out
+
+        def outputs(idx: str, ind: str) -> list:
+            out = []
+            for slot, total in totals():
                 if slot == self.slot:
                     out.append(f"{ind}p.lam_out[{idx}] = {total};")
                 else:
@@ -394,8 +400,25 @@ class AdjointGenerator:
             L += ["    }", "  }"]
             return L
 
-        K = [f"template <typename I> __global__ void __launch_bounds__(256, {ZWALK_BLOCKS if zwalk else 4}) xgk_{n}_adjoint("
-             f"const __grid_constant__ struct xgadj_{n} p) {{"] + TILE_PROLOGUE
+        # staged z-walk (planes of lam', u and the coefficients streamed through shared
+        # memory): every offset within one cell on every axis
+        staged = zwalk and all(max(abs(c) for c in o) <= 1 for _, offs in bufs.values() for o in offs)
+        S = []
+        if staged:
+            keys = list(bufs)
+            zl = []
+            for i, off in enumerate(lam_offsets):
+                names[("lam", off)] = f"a{i}"
+                zl.append((f"a{i}", keys.index("lam"), off))
+            for i, key in enumerate(loads_needed):
+                slot, level, off = key
+                names[key] = f"v{i}"
+                zl.append((f"v{i}", keys.index((slot, level)), off))
+            zo = [("p.lam_out", tot, None, False) if slot == self.slot else (f"p.g{slot}", tot, f"p.g{slot}", True)
+                  for slot, tot in totals()]
+            S = [zstage_frame(f"xgk_{n}_adjoint_zs", f"struct xgadj_{n}", T, [bufs[k][0] for k in keys], zl, zo)]
+        K = S + [f"template <typename I> __global__ void __launch_bounds__(256, {ZWALK_BLOCKS if zwalk else 4}) "
+                 f"xgk_{n}_adjoint(const __grid_constant__ struct xgadj_{n} p) {{"] + TILE_PROLOGUE
         if zwalk:
             K += zwalk_body() + ["}"]
         else:
@@ -426,6 +449,12 @@ class AdjointGenerator:
             for lv in range(gen.depth + 1):
                 H.append(f"  p.f{slot}[{lv}] = (const {T}*)fields[{slot} * {gen.depth + 1} + {lv}];")
             H.append(f"  p.g{slot} = ({T}*)grads[{slot}];")
+        if staged:
+            H += [f"  if (xg_adjoint_zstage_{n})"]
+            H += zstage_launch(f"xgk_{n}_adjoint_zs", T, len(bufs), "  ",
+                               [bufs[k][0] for k in bufs] + ["p.lam_out"] + [f"p.g{sl}" for sl in slots_used
+                                                                             if sl != self.slot],
+                               ["xg_prof_launch(-2, s);"], ["xg_prof_end(-2, s);"])
         tz, ty, tx, bx, by = ZWALK_TILE if zwalk else (2, 16, 32, 32, 8)
         H += [f"  p.tz = {tz}; p.ty = {ty}; p.tx = {tx};",
               "  p.ntz = xg_tiles_along(p.Z, p.tz); p.nty = xg_tiles_along(p.Y, p.ty); p.ntx = xg_tiles_along(p.X, p.tx);",
@@ -447,8 +476,10 @@ class AdjointGenerator:
             ga.append("  char xg_empty;")
         ga.append("};")
         structs = gen.struct_defs()
+        sw = [f"static int xg_adjoint_zstage_{n} = 1;  // staged z-walk of the adjoint step (0: register z-walk)",
+              f'extern "C" int xg_adjoint_zstage_set_{n}(int on) {{ xg_adjoint_zstage_{n} = on; return 0; }}']
         src = ['#include "xgrid_gen.cuh"', f"static const int xg_overstep = {gen.mode};"] + structs + ga + hs + \
-            lines + K + H
+            lines + K + sw + H
         return "\n".join(src) + "\n", f"xg_adjoint_{n}"
 
 
@@ -503,6 +534,15 @@ class Rollout:
         self.order = m.arg_order
         self.grids = None
 
+    def set_zstage(self, on: bool) -> None:
+        """Staged z-walks (planes streamed through shared memory, the default) or
+        register z-walks for the forward and the adjoint steps."""
+        self.native.set_zstage(on)
+        fn = getattr(self.meta["lib"].dylib, f"xg_adjoint_zstage_set_{self.native.module.name}", None)
+        if fn is not None:
+            fn.restype = ctypes.c_int
+            fn(ctypes.c_int(1 if on else 0))
+
     def _grids(self, shape, dtype_type):
         from .grid import Grid
         if self.grids is None or self.grids[self.target].shape != tuple(shape):
@@ -552,10 +592,21 @@ def _make_function():
     torch = _torch()
     from . import device, runtime
 
+    def _hand_back(caller, s, tensors):
+        # results made on the backend stream are read on the caller's stream: order the
+        # caller after the backend's work, and tell the caching allocator about the use
+        caller.wait_stream(s)
+        for t in tensors:
+            t.record_stream(caller)
+
     class Fn(torch.autograd.Function):
         @staticmethod
         def forward(ctx, plan, values, u0, *coefs):
             s = device.stream()
+            caller = torch.cuda.current_stream()
+            s.wait_stream(caller)  # the inputs may still be in production on the caller's stream
+            for t in (u0, *coefs):
+                t.record_stream(s)
             names = plan.coef_names(dict.fromkeys(plan.grid_names))
             with torch.cuda.stream(s):
                 ftype = float
@@ -576,6 +627,7 @@ def _make_function():
                     if done < plan.steps:
                         checkpoints.append(ug.tensor(0).clone())
                 out = ug.tensor(0).clone()
+            _hand_back(caller, s, [out])
             ctx.plan, ctx.values, ctx.names = plan, values, names
             ctx.checkpoints = checkpoints
             ctx.save_for_backward(*coefs)
@@ -586,6 +638,10 @@ def _make_function():
             plan, values, names = ctx.plan, ctx.values, ctx.names
             coefs = ctx.saved_tensors
             s = device.stream()
+            caller = torch.cuda.current_stream()
+            s.wait_stream(caller)
+            for t in (grad_out, *coefs):
+                t.record_stream(s)
             with torch.cuda.stream(s):
                 grids = plan._grids(grad_out.shape, float)
                 ug = grids[plan.target]
@@ -621,6 +677,7 @@ def _make_function():
                         if rc != 0:
                             LOG.dead(f"adjoint kernel failed: {runtime.last_error()}")
                         lam = new
+            _hand_back(caller, s, [lam] + list(gcoef.values()))
             return (None, None, lam) + tuple(gcoef[n] for n in names)
 
     return Fn

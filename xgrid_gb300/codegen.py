@@ -47,9 +47,10 @@ OVERSTEP = {"none": "XG_OVERSTEP_NONE", "limit": "XG_OVERSTEP_LIMIT", "wrap": "X
 ZWALK_PLANES = 4
 ZWALK_BLOCKS = 4
 
-# staged z-walk of mask-free 3-D sweeps: (z, y, x) tile, thread rows, planes prefetched
-ZSTAGE_TILE = (32, 16, 64)
-ZSTAGE_BY = 4
+# staged z-walk of mask-free 3-D sweeps: (y, x) column block of a CTA, thread rows, planes
+# prefetched beyond the next one (chunk lengths along z: xg_zstage_chunks)
+ZSTAGE_TILE = (16, 64)
+ZSTAGE_THREADS = 256
 ZSTAGE_AHEAD = 2
 
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
@@ -537,6 +538,7 @@ class CudaGenerator:
         src.append("};")
         src.append(f"static int xg_fuse_{name} = {1 if self.cfg.fuse else 0};")
         src.append(f"static int xg_zstage_{name} = 1;  // staged z-walk of mask-free 3-D sweeps (0: register z-walk)")
+        src.append(f"static long long xg_zstage_launches_{name} = 0;  // staged z-walk launches issued by the host")
         # launch hook (slab decomposition): called before every single-sweep launch with the
         # launch's site (group * 64 + sweep), so that a caller can refresh halo rows first
         src.append(f"static xg_launch_hook_fn xg_hook_{name} = NULL;")
@@ -566,6 +568,7 @@ class CudaGenerator:
         src.append("}")
         src.append(f'extern "C" int xg_groups_{name}(void) {{ return {self.group_counter[0]}; }}')
         src.append(f'extern "C" int xg_zstage_set_{name}(int on) {{ xg_zstage_{name} = on; return 0; }}')
+        src.append(f'extern "C" long long xg_zstage_launches_get_{name}(void) {{ return xg_zstage_launches_{name}; }}')
         src.append(f'extern "C" int xg_set_hook_{name}(xg_launch_hook_fn fn, void* ctx) {{')
         src.append(f"  xg_hook_{name} = fn;")
         src.append(f"  xg_hook_ctx_{name} = ctx;")
@@ -895,6 +898,233 @@ def has_stencil(e) -> bool:
 def unsafe_int_div(e) -> bool:
     return any(isinstance(n, ir.Binary) and n.operator in (ir.BinaryOperator.Div, ir.BinaryOperator.Mod)
                and isinstance(n.type, Integer) for n in ir.walk(e))
+
+
+def zstage_geometry(T: str, nb: int) -> dict:
+    """Shape of a staged z-walk CTA for element type ``T`` and ``nb`` staged
+    buffers: V cells per 16-byte vector, NTX x NTY threads, RY rows per thread,
+    plane rows of PX = TX + 2V elements (cell x0 at column V, halo at V - 1 and
+    V + TX), D planes beyond the next one in flight (one when three or more
+    buffers share the ring, so that three CTAs fit on an SM)."""
+    ty, tx = ZSTAGE_TILE
+    size = 8 if T == "double" else 4
+    v = 16 // size
+    ntx = tx // v
+    nty = ZSTAGE_THREADS // ntx
+    d = ZSTAGE_AHEAD if nb <= 2 else 1
+    px = tx + 2 * v
+    smem = (d + 3) * nb * (ty + 2) * px * size
+    # CTAs per SM that the shared memory allows (228 KiB per SM, 1 KiB reserved per CTA), at most 3:
+    # the register budget ptxas gets follows from it
+    blocks = max(1, min(3, (228 * 1024) // (smem + 1024)))
+    return {"V": v, "NTX": ntx, "NTY": nty, "RY": ty // nty, "D": d, "PX": px, "TY": ty, "TX": tx,
+            "smem": smem, "size": size, "blocks": blocks}
+
+
+def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: list) -> str:
+    """A staged z-walk kernel.  Each CTA owns a (TY, TX) column block of a chunk
+    of ``zlen`` planes (a launch argument) and streams the planes z0-1 .. z1 of
+    every source buffer, block plus a one-cell halo (wrapped or clamped), through
+    a ring of shared-memory slots with cp.async, D planes beyond the next one in
+    flight; 16-byte copies where the block's rows and halo lie inside the grid
+    and ``vec`` says the rows are 16-byte aligned, element copies otherwise.
+    Every thread owns a 16-byte vector of V consecutive cells in RY rows: per
+    plane it reads each needed row of each buffer as one vector from shared
+    memory, plus the single cells left and right of it, and computes its V cells
+    one by one with the scalar expression (same arithmetic per cell as the
+    other paths); results leave as one 16-byte store per row when ``vec``.
+
+    ``loads``: (variable, source index, (oz, oy, ox)), offsets within one cell;
+    ``outs``: (destination pointer, value, guard or None, accumulate) -- the cell
+    value (an expression of the load variables) is stored, or added to the
+    destination's value when ``accumulate``; a guard skips the output when it
+    is null.  The parameter struct has Z, Y, X."""
+    g = zstage_geometry(T, len(srcs))
+    V, NTX, NTY, RY, D, PX, TY, TX = (g[k] for k in ("V", "NTX", "NTY", "RY", "D", "PX", "TY", "TX"))
+    VT = "double2" if T == "double" else "float4"
+    nb = len(srcs)
+    comp = "xyzw"
+    K = [f"template <typename I> __global__ void __launch_bounds__({ZSTAGE_THREADS}, {g['blocks']}) "
+         f"{kname}(const __grid_constant__ {ptype} p, const int zlen, const int vec) {{",
+         f"  constexpr int TY = {TY}, TX = {TX}, V = {V}, NTX = {NTX}, NT = {ZSTAGE_THREADS}, D = {D};",
+         f"  constexpr int PX = {PX}, PY = TY + 2, PL = PY * PX, R = D + 3, NB = {nb};",
+         "  constexpr int KV = (PL / V + NT - 1) / NT, KE = (PL + NT - 1) / NT;",
+         "  extern __shared__ __align__(16) unsigned char xg_zs_raw[];",
+         f"  {T}* const ring = ({T}*)xg_zs_raw;  // [R][NB][PY][PX]",
+         "  const int tid = threadIdx.x;",
+         "  const int ntx = (int)((p.X + TX - 1) / TX), nty = (int)((p.Y + TY - 1) / TY);",
+         "  const int ix = blockIdx.x % ntx, iy = (blockIdx.x / ntx) % nty, iz = blockIdx.x / (ntx * nty);",
+         "  const int x0 = ix * TX, y0 = iy * TY, z0 = iz * zlen;",
+         "  const int z1 = z0 + zlen < (int)p.Z ? z0 + zlen : (int)p.Z;",
+         "  const I sy = (I)p.X, sz = (I)(p.X * p.Y);",
+         "  // 16-byte staging: the rows x0 - V .. x0 + TX + V - 1 lie inside the grid",
+         "  const bool vst = vec && x0 >= V && x0 + TX + V <= (int)p.X;",
+         "  // this thread's staging copies: their (wrapped or clamped) element offsets in a plane, -1 = none",
+         "  I goff[KE];",
+         "#pragma unroll",
+         "  for (int k = 0; k < KE; ++k) {",
+         "    const int e = tid + k * NT;",
+         "    goff[k] = -1;",
+         "    if (vst) {",
+         "      if (k < KV && e < PL / V) {",
+         "        const int r = (e * V) / PX, c = (e * V) % PX;",
+         "        goff[k] = (I)xg_axis(xg_overstep, y0 - 1 + r, (int)p.Y) * sy + (I)(x0 - V + c);",
+         "      }",
+         "    } else if (e < PL) {",
+         "      const int r = e / PX, c = e % PX;",
+         "      if (c >= V - 1 && c <= V + TX)",
+         "        goff[k] = (I)xg_axis(xg_overstep, y0 - 1 + r, (int)p.Y) * sy + "
+         "(I)xg_axis(xg_overstep, x0 - V + c, (int)p.X);",
+         "    }",
+         "  }",
+         f"  const {T}* const src[NB] = {{{', '.join(srcs)}}};",
+         "  auto stage = [&](int q) {  // plane q into its ring slot (no copies for q beyond the chunk)",
+         "    if (q <= z1) {",
+         "      const I zb = (I)xg_axis(xg_overstep, q, (int)p.Z) * sz;",
+         f"      {T}* const slot = ring + ((q - z0 + 1) % R) * NB * PL;",
+         "      if (vst) {",
+         "#pragma unroll",
+         "        for (int b = 0; b < NB; ++b)",
+         "#pragma unroll",
+         "          for (int k = 0; k < KV; ++k)",
+         "            if (goff[k] >= 0) xg_cp_async16(slot + b * PL + (tid + k * NT) * V, src[b] + zb + goff[k]);",
+         "      } else {",
+         "#pragma unroll",
+         "        for (int b = 0; b < NB; ++b)",
+         "#pragma unroll",
+         "          for (int k = 0; k < KE; ++k)",
+         "            if (goff[k] >= 0) xg_cp_async(slot + b * PL + tid + k * NT, src[b] + zb + goff[k]);",
+         "      }",
+         "    }",
+         "    xg_cp_async_commit();",
+         "  };",
+         "#pragma unroll",
+         "  for (int q = 0; q < R - 1; ++q) stage(z0 - 1 + q);",
+         "  const int tx_t = tid % NTX, ty_t = tid / NTX;",
+         "  const int c0 = V + V * tx_t, x = x0 + V * tx_t;  // the thread's first cell: ring column, grid x",
+         "  XG_ZSTAGE_WINDOW",
+         "  for (int z = z0; z < z1; ++z) {",
+         "    stage(z + D + 1);  // into the slot plane z - 2 used (freed by the barrier below)",
+         "    xg_cp_async_wait_group<D>();  // planes up to z + 1 have landed",
+         "    __syncthreads();",
+         f"    const {T}* const pl_m = ring + ((z - z0) % R) * NB * PL;      // plane z - 1",
+         f"    const {T}* const pl_c = ring + ((z - z0 + 1) % R) * NB * PL;  // plane z",
+         f"    const {T}* const pl_p = ring + ((z - z0 + 2) % R) * NB * PL;  // plane z + 1",
+         "    (void)pl_m; (void)pl_p;",
+         "#pragma unroll",
+         f"    for (int i = 0; i < {RY}; ++i) {{",
+         f"      const int r = ty_t + i * {NTY} + 1, y = y0 + r - 1;",
+         "      if (y < (int)p.Y && x < (int)p.X) {",
+         "        const I gb = (I)z * sz + (I)y * sy + (I)x;"]
+    # rows of the ring this thread reads: (buffer, oz, oy) -> which of x-1 / x+V it needs too
+    rows = {}
+    for _, b, (oz, oy, ox) in loads:
+        need = rows.setdefault((b, oz, oy), set())
+        need.add(ox)
+    plane = {-1: "pl_m", 0: "pl_c", 1: "pl_p"}
+    zw = sorted({b for (b, oz, oy) in rows if oz == 1 and oy == 0})
+    if zw:
+        K.append("        if (z == z0) {  // the window's first planes")
+        for b in zw:
+            for nm, pl in (("m", "pl_m"), ("c", "pl_c")):
+                K.append(f"          zw{b}_{nm}[i] = *reinterpret_cast<const {VT}*>(&{pl}[{b} * PL + r * PX + c0]);")
+        K.append("        }")
+
+    def rn(b, oz, oy):
+        return f"w{b}_{'m' if oz < 0 else ('p' if oz > 0 else 'c')}{'m' if oy < 0 else ('p' if oy > 0 else 'c')}"
+    # buffers read at the next plane's centre row keep their centre rows of planes z - 1
+    # and z in registers (a window shifted by one plane per step)
+    zwin = sorted({b for (b, oz, oy) in rows if oz == 1 and oy == 0})
+    for (b, oz, oy), oxs in rows.items():
+        base = f"{plane[oz]}[{b} * PL + (r + ({oy})) * PX + c0"
+        w = rn(b, oz, oy)
+        if b in zwin and oy == 0 and oz <= 0:
+            K.append(f"        const {VT} {w} = zw{b}_{'m' if oz < 0 else 'c'}[i];")
+        else:
+            K.append(f"        const {VT} {w} = *reinterpret_cast<const {VT}*>(&{base}]);")
+        if -1 in oxs:
+            K.append(f"        const {T} {w}_l = {base} - 1];")
+        if 1 in oxs:
+            K.append(f"        const {T} {w}_r = {base} + V];")
+    for o, _ in enumerate(outs):
+        K.append(f"        {T} o{o}[V];")
+    for j in range(V):
+        K.append("        {")
+        for vn, b, (oz, oy, ox) in loads:
+            w = rn(b, oz, oy)
+            jj = j + ox
+            val = f"{w}_l" if jj < 0 else (f"{w}_r" if jj >= V else f"{w}.{comp[jj]}")
+            K.append(f"          const {T} {vn} = {val};")
+        K.append(f"          const I gi = gb + {j};")
+        K.append("          (void)gi;")
+        for o, (_, value, _, _) in enumerate(outs):
+            K.append(f"          o{o}[{j}] = {value};")
+        K.append("        }")
+    K.append("        if (vec) {  // one 16-byte store per output")
+    for o, (dst, _, guard, acc) in enumerate(outs):
+        ind = "          "
+        if guard:
+            K.append(f"{ind}if ({guard}) {{")
+            ind += "  "
+        vals = ", ".join(f"o{o}[{j}]" for j in range(V))
+        if acc:
+            K.append(f"{ind}{VT} a = *reinterpret_cast<const {VT}*>(&{dst}[gb]);")
+            vals = ", ".join(f"a.{comp[j]} + (o{o}[{j}])" for j in range(V))
+        K.append(f"{ind}*reinterpret_cast<{VT}*>(&{dst}[gb]) = make_{VT}({vals});")
+        if guard:
+            K.append("          }")
+    K.append("        } else {")
+    K.append("#pragma unroll")
+    K.append("          for (int j = 0; j < V; ++j)")
+    K.append("            if (x + j < (int)p.X) {")
+    for o, (dst, _, guard, acc) in enumerate(outs):
+        pre = f"if ({guard}) " if guard else ""
+        if acc:
+            K.append(f"              {pre}{dst}[gb + j] = {dst}[gb + j] + (o{o}[j]);")
+        else:
+            K.append(f"              {pre}{dst}[gb + j] = o{o}[j];")
+    K += ["            }",
+          "        }"]
+    for b in zw:
+        K += [f"        zw{b}_m[i] = zw{b}_c[i];", f"        zw{b}_c[i] = {rn(b, 1, 0)};"]
+    K += ["      }",
+          "    }",
+          "    __syncthreads();  // the slot of plane z - 1 is free for plane z + D + 2",
+          "  }",
+          "  xg_cp_async_wait_all();",
+          "}"]
+    decl = " ".join(f"{VT} zw{b}_m[{RY}], zw{b}_c[{RY}];" for b in zw)
+    K = [line.replace("  XG_ZSTAGE_WINDOW", f"  {decl}" if decl else "") for line in K]
+    return "\n".join(line for line in K if line)
+
+
+def zstage_launch(kname: str, T: str, nb: int, ind: str, aligned: list, before: list, after: list) -> list:
+    """Host lines launching ``kname`` (a ``zstage_frame`` kernel) with parameters
+    ``p`` on stream ``s`` when its shared memory fits; ``aligned``: the pointers
+    (sources and destinations) that must be 16-byte aligned for 16-byte copies;
+    ``before`` / ``after`` run around the launch, which ends with ``return 0``.
+    Falls through otherwise."""
+    g = zstage_geometry(T, nb)
+    ty, tx = ZSTAGE_TILE
+    al = " && ".join(f"((uintptr_t)({a}) & 15) == 0" for a in aligned) or "1"
+    L = ["{",
+         f"  const size_t smem = {g['smem']};",
+         "  static int avail32 = -1, avail64 = -1;",
+         "  const bool small = xg_small_index(p.Z, p.Y, p.X);",
+         f"  if (small && avail32 < 0) XG_TRY(xg_smem_optin({kname}<int>, &avail32));",
+         f"  if (!small && avail64 < 0) XG_TRY(xg_smem_optin({kname}<int64_t>, &avail64));",
+         "  int zlen = 0;",
+         "  int64_t nt = 0;",
+         f"  XG_TRY(xg_zstage_chunks(p.Z, p.Y, p.X, {ty}, {tx}, &zlen, &nt));",
+         f"  const int vec = (p.X % {g['V']}) == 0 && {al};",
+         "  if (smem <= (size_t)(small ? avail32 : avail64) && nt <= 0x7fffffffLL) {"]
+    L += ["    " + b for b in before]
+    L += [f"    if (small) {kname}<int><<<(unsigned)nt, {ZSTAGE_THREADS}, smem, s>>>(p, zlen, vec);",
+          f"    else {kname}<int64_t><<<(unsigned)nt, {ZSTAGE_THREADS}, smem, s>>>(p, zlen, vec);",
+          "    XG_CUDA(cudaGetLastError());"]
+    L += ["    " + a for a in after]
+    L += ["    return 0;", "  }", "}"]
+    return [ind + line for line in L]
 
 
 class SweepGroupEmitter:
@@ -1576,93 +1806,23 @@ class SweepGroupEmitter:
         return bufs
 
     def zstage_kernel(self, tag: str, j: int, bufs: list) -> str:
-        """Staged z-walk: each CTA owns a (ty, tx) column block of a z chunk and
-        streams the planes z0-1 .. z1 of every read buffer, block plus a one-cell
-        halo, through a ring of shared-memory slots with cp.async (``ZSTAGE_AHEAD``
-        planes beyond the next one in flight); plane z reads its horizontal
-        neighbours and the planes above and below from the ring.  Same arithmetic
-        per cell as the other paths."""
+        """Staged z-walk of sweep ``j`` (``zstage_frame``): same arithmetic per
+        cell as the other paths."""
         n, gid = self.name, self.gid
         s = self.g.sweeps[j]
         T = self.elem(bufs[0][0])
-        tz, ty, tx = ZSTAGE_TILE
         dst = self.bname((s.slot, s.level, s.write_version))
-        nb = len(bufs)
         names, local = {}, {}
-        pre = []
+        loads = []
         for st, ld in s.loads:
             if ld not in local:
-                vn = f"l{len(local)}"
-                local[ld] = vn
-                b = bufs.index((ld.slot, ld.level, ld.version))
-                oz, oy, ox = ld.offset
-                slot = "pl_c" if oz == 0 else ("pl_m" if oz < 0 else "pl_p")
-                pre.append(f"        const {T} {vn} = {slot}[{b} * PL + (r + ({oy})) * PX + (c + ({ox}))];")
+                local[ld] = f"l{len(local)}"
+                loads.append((local[ld], bufs.index((ld.slot, ld.level, ld.version)), ld.offset))
             names[id(st)] = local[ld]
         env = SweepEnv(self.gen, self.hoist_map, names, self.div_map, self.mul_map)
         val = self.gen.expr(s.stmt.value, env)
-        K = [f"template <typename I> __global__ void __launch_bounds__({tx * ZSTAGE_BY}, 3) "
-             f"xgk_{n}_{gid}_{tag}_zs(const __grid_constant__ struct xgp_{n}_{gid}_{tag} p) {{",
-             f"  constexpr int TZ = {tz}, TY = {ty}, TX = {tx}, BY = {ZSTAGE_BY}, RY = TY / BY, D = {ZSTAGE_AHEAD};",
-             "  constexpr int PX = TX + 2, PY = TY + 2, PL = PY * PX, R = D + 3, NT = TX * BY;",
-             f"  constexpr int NB = {nb}, KE = (PL + NT - 1) / NT;",
-             f"  extern __shared__ __align__(16) unsigned char xg_zs_raw[];",
-             f"  {T}* const ring = ({T}*)xg_zs_raw;  // [R][NB][PL]",
-             "  const int tid = threadIdx.x + TX * threadIdx.y;",
-             "  const int ntx = (int)((p.X + TX - 1) / TX), nty = (int)((p.Y + TY - 1) / TY);",
-             "  const int ix = blockIdx.x % ntx, iy = (blockIdx.x / ntx) % nty, iz = blockIdx.x / (ntx * nty);",
-             "  const int x0 = ix * TX, y0 = iy * TY, z0 = iz * TZ;",
-             "  const int z1 = z0 + TZ < (int)p.Z ? z0 + TZ : (int)p.Z;",
-             "  const I sy = (I)p.X, sz = (I)(p.X * p.Y);",
-             "  // this thread's staging elements: their (wrapped or clamped) offsets in a plane",
-             "  I goff[KE];",
-             "#pragma unroll",
-             "  for (int k = 0; k < KE; ++k) {",
-             "    const int e = tid + k * NT;",
-             "    const int ey = (e < PL ? e / PX : 0) - 1 + y0, ex = (e < PL ? e % PX : 0) - 1 + x0;",
-             "    goff[k] = (I)xg_axis(xg_overstep, ey, (int)p.Y) * sy + (I)xg_axis(xg_overstep, ex, (int)p.X);",
-             "  }"]
-        srcs = ", ".join(f"p.{self.bname(b)}" for b in bufs)
-        K += [f"  const {T}* const src[NB] = {{{srcs}}};",
-              "  auto stage = [&](int q) {  // plane q into its ring slot (no copies for q beyond the chunk)",
-              "    if (q <= z1) {",
-              "      const I zb = (I)xg_axis(xg_overstep, q, (int)p.Z) * sz;",
-              f"      {T}* const slot = ring + ((q - z0 + 1) % R) * NB * PL;",
-              "#pragma unroll",
-              "      for (int b = 0; b < NB; ++b)",
-              "#pragma unroll",
-              "        for (int k = 0; k < KE; ++k) {",
-              "          const int e = tid + k * NT;",
-              "          if (e < PL) xg_cp_async(slot + b * PL + e, src[b] + zb + goff[k]);",
-              "        }",
-              "    }",
-              "    xg_cp_async_commit();",
-              "  };",
-              "#pragma unroll",
-              "  for (int q = 0; q < R - 1; ++q) stage(z0 - 1 + q);",
-              f"  {T}* __restrict__ out = p.{dst};",
-              "  for (int z = z0; z < z1; ++z) {",
-              "    stage(z + D + 1);  // into the slot plane z - 2 used (freed by the barrier below)",
-              "    xg_cp_async_wait_group<D>();  // planes up to z + 1 have landed",
-              "    __syncthreads();",
-              f"    const {T}* const pl_m = ring + ((z - z0) % R) * NB * PL;      // plane z - 1",
-              f"    const {T}* const pl_c = ring + ((z - z0 + 1) % R) * NB * PL;  // plane z",
-              f"    const {T}* const pl_p = ring + ((z - z0 + 2) % R) * NB * PL;  // plane z + 1",
-              "    (void)pl_m; (void)pl_p;",
-              "    const int c = threadIdx.x + 1, x = x0 + (int)threadIdx.x;",
-              "#pragma unroll",
-              "    for (int i = 0; i < RY; ++i) {",
-              "      const int r = threadIdx.y + i * BY + 1, y = y0 + r - 1;",
-              "      if (x < (int)p.X && y < (int)p.Y) {"]
-        K += pre
-        K += [f"        out[(I)z * sz + (I)y * sy + (I)x] = {val};",
-              "      }",
-              "    }",
-              "    __syncthreads();  // the slot of plane z - 1 is free for plane z + D + 2",
-              "  }",
-              "  xg_cp_async_wait_all();",
-              "}"]
-        return "\n".join(K)
+        return zstage_frame(f"xgk_{n}_{gid}_{tag}_zs", f"struct xgp_{n}_{gid}_{tag}", T,
+                            [f"p.{self.bname(b)}" for b in bufs], loads, [(f"p.{dst}", val, None, False)])
 
     def emit_main_single(self, j: int, s) -> None:
         n, gid = self.name, self.gid
@@ -1689,34 +1849,19 @@ class SweepGroupEmitter:
                      f"p.e{s.slot}[2]) * sizeof(*p.{dst}), cudaMemcpyDeviceToDevice, s));")
         site = gid * 64 + j
         if zbufs:
-            tz, ty, tx = ZSTAGE_TILE
-            T = self.elem(zbufs[0][0])
-            smem = (ZSTAGE_AHEAD + 3) * len(zbufs) * (ty + 2) * (tx + 2)
             # a grid without boundary cells takes the staged z-walk (every tile mask-free)
             L += [f"  if (p.same && xg_zstage_{n}) {{",
                   "    int64_t nz = 0;",
                   f"    XG_TRY(xg_mask_nonzero(G[{s.slot}].mask, &nz));",
-                  "    if (nz == 0) {",
-                  f"      const size_t smem = (size_t){smem} * sizeof({T});",
-                  "      static int avail32 = -1, avail64 = -1;",
-                  "      const bool small = xg_small_index(p.Z, p.Y, p.X);",
-                  f"      if (small && avail32 < 0) XG_TRY(xg_smem_optin(xgk_{n}_{gid}_{tag}_zs<int>, &avail32));",
-                  f"      if (!small && avail64 < 0) XG_TRY(xg_smem_optin(xgk_{n}_{gid}_{tag}_zs<int64_t>, &avail64));",
-                  "      if (smem <= (size_t)(small ? avail32 : avail64)) {",
-                  f"        const int64_t nt = ((p.X + {tx - 1}) / {tx}) * ((p.Y + {ty - 1}) / {ty}) * "
-                  f"((p.Z + {tz - 1}) / {tz});",
-                  "        if (nt <= 0x7fffffffLL) {",
-                  f"          if (xg_hook_{n}) XG_TRY(xg_hook_{n}(xg_hook_ctx_{n}, {site}, G, {len(self.gen.slots)}, s));",
-                  f"          xg_prof_launch({site}, s);",
-                  f"          if (small) xgk_{n}_{gid}_{tag}_zs<int><<<(unsigned)nt, dim3({tx}, {ZSTAGE_BY}), smem, s>>>(p);",
-                  f"          else xgk_{n}_{gid}_{tag}_zs<int64_t><<<(unsigned)nt, dim3({tx}, {ZSTAGE_BY}), smem, s>>>(p);",
-                  "          XG_CUDA(cudaGetLastError());",
-                  f"          xg_prof_end({site}, s);",
-                  "          return 0;",
-                  "        }",
-                  "      }",
-                  "    }",
-                  "  }"]
+                  "    if (nz == 0)"]
+            dst = self.bname((s.slot, s.level, s.write_version))
+            L += zstage_launch(f"xgk_{n}_{gid}_{tag}_zs", self.elem(zbufs[0][0]), len(zbufs), "    ",
+                               [f"p.{self.bname(b)}" for b in zbufs] + [f"p.{dst}"],
+                               [f"if (xg_hook_{n}) XG_TRY(xg_hook_{n}(xg_hook_ctx_{n}, {site}, G, "
+                                f"{len(self.gen.slots)}, s));", f"xg_prof_launch({site}, s);",
+                                f"++xg_zstage_launches_{n};"],
+                               [f"xg_prof_end({site}, s);"])
+            L += ["  }"]
         L += ["  dim3 block(tl[3], tl[4], tl[5]), grid;",
               "  XG_TRY(xg_tile_grid(p.ntx, p.nty, p.ntz, &grid));",
               f"  if (xg_hook_{n}) XG_TRY(xg_hook_{n}(xg_hook_ctx_{n}, {site}, G, {len(self.gen.slots)}, s));",

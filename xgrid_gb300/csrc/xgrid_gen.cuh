@@ -584,6 +584,38 @@ static inline int xg_smem_optin(K* kernel, int* avail) {
   return 0;
 }
 
+// Chunk length along z of a staged z-walk launch over a Z x Y x X grid cut into
+// (ty, tx) column blocks, one CTA per (block, chunk): the chunk count per column
+// minimises ceil(CTAs / SMs) * (planes per chunk + 1), the planes that the
+// busiest SM streams when every CTA costs its own planes plus its two halo
+// planes at half weight (neighbouring chunks read them too, often from L2).
+// Chunks hold at least 8 planes.  *nt receives the CTA count.
+static inline int xg_zstage_chunks(int64_t Z, int64_t Y, int64_t X, int ty, int tx, int* zlen, int64_t* nt) {
+  static int nsm = 0;
+  if (nsm == 0) {
+    int dev = 0;
+    XG_CUDA(cudaGetDevice(&dev));
+    XG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    if (nsm < 1) nsm = 1;
+  }
+  const int64_t ncb = ((X + tx - 1) / tx) * ((Y + ty - 1) / ty);
+  int64_t cmax = Z / 8 > 1 ? Z / 8 : 1;
+  if (cmax > 4096) cmax = 4096;
+  int64_t best_len = Z, best_cost = -1;
+  for (int64_t c = 1; c <= cmax; ++c) {
+    const int64_t len = (Z + c - 1) / c, chunks = (Z + len - 1) / len;
+    const int64_t cost = ((ncb * chunks + nsm - 1) / nsm) * (len + 1);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best_len = len;
+    }
+  }
+  if (best_len > 0x7fffffffLL) XG_FAIL("staged z-walk: chunk of %lld planes", (long long)best_len);
+  *zlen = (int)best_len;
+  *nt = ncb * ((Z + best_len - 1) / best_len);
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
 // Binary64 addition on the integer pipe.
 //
@@ -652,6 +684,13 @@ __device__ __forceinline__ void xg_cp_async(T* dst, const T* src) {
   static_assert(sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "cp.async copies 4, 8 or 16 bytes");
   asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(xg_smem_addr(dst)), "l"(src), "n"(sizeof(T))
                : "memory");
+}
+
+// 16 bytes from global to shared memory, both 16-byte aligned, through L2 only
+// (cp.async.cg): staged planes are read once per CTA.
+template <typename T>
+__device__ __forceinline__ void xg_cp_async16(T* dst, const T* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(xg_smem_addr(dst)), "l"(src) : "memory");
 }
 
 __device__ __forceinline__ void xg_cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }

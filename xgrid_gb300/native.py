@@ -69,6 +69,13 @@ class NativeKernel:
         fn(ctypes.c_int(1 if on else 0))
         runtime.load().xg_graph_clear(self.fn_ptr)
 
+    def zstage_launches(self) -> int:
+        """Staged z-walk launches this module's host code has issued (graph
+        replays re-run captured launches without counting)."""
+        fn = getattr(self.lib.dylib, f"xg_zstage_launches_get_{self.module.name}")
+        fn.restype = ctypes.c_longlong
+        return int(fn())
+
     def set_mixed_every(self, every: int) -> None:
         """Iterations between FP64 corrections of mixed-precision loops (0 = once per loop)."""
         self.mixed_fn(int(every))
