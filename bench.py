@@ -934,8 +934,9 @@ def batch_section(count: int, steps: int, seq_steps: int) -> dict:
 
 def adjoint_section(n: int, steps: int, every: int, torch_n: int, cpu_n: int = 64) -> dict:
     """3-D variable-coefficient diffusion, FP32, periodic: forward rollout and its
-    gradient w.r.t. the initial field and the diffusivity (adjoint kernels with
-    checkpoints every ``every`` steps).  Compared with PyTorch autograd through
+    gradient w.r.t. the initial field and the diffusivity (adjoint kernels; the
+    forward pass keeps every state when ``every`` is 1, else a checkpoint every
+    ``every`` steps, and the checkpointed variant is timed beside it).  Compared with PyTorch autograd through
     the same stencil on tensors: on the GPU at ``torch_n``^3, and on all host
     cores at ``cpu_n``^3 (the CPU baseline; the reference mis-indexes 3-D grids).
     ``e2e``: host arrays in, loss gradient arrays out."""
@@ -951,10 +952,10 @@ def adjoint_section(n: int, steps: int, every: int, torch_n: int, cpu_n: int = 6
                opt_level=3, overstep="wrap")
     k = Operator(workloads.diffuse3d.func, "kernel", "diffuse3d")
 
-    def run_ours(m, nsteps, host=False):
+    def run_ours(m, nsteps, host=False, interval=every):
         u0, kap, tgt, dt = workloads.adjoint_setup(m, 2)
         dev = [torch.tensor(x, device="cuda") for x in (u0, kap, tgt)]
-        ro = adjoint.Rollout(k, nsteps, every)
+        ro = adjoint.Rollout(k, nsteps, interval)
         a, bb = dev[0].clone().requires_grad_(True), dev[1].clone().requires_grad_(True)
         s = device.stream()
         # warm-up (compile, tables)
@@ -986,16 +987,29 @@ def adjoint_section(n: int, steps: int, every: int, torch_n: int, cpu_n: int = 6
     f, bwd, loss = run_ours(n, steps)
     cells = n ** 3
     hbm, src = peaks()
-    out = {"config": f"{n}^3 FP32 periodic, {steps} steps, checkpoint every {every}, loss MSE to a random target",
+    kept = "every state kept (state pool in HBM)" if every == 1 else f"checkpoint every {every}"
+    recomputed = 0 if every == 1 else steps - (steps + every - 1) // every
+    out = {"config": f"{n}^3 FP32 periodic, {steps} steps, {kept}, loss MSE to a random target",
            "forward_s": f, "backward_s": bwd, "loss": loss,
            "forward_glups": cells * steps / f / 1e9, "forward_gbs": 12.0 * cells * steps / f / 1e9,
            "backward_glups": cells * steps / bwd / 1e9,
-           "backward_note": f"backward = {steps - (steps + every - 1) // every} recomputed forward steps + "
-                            f"{steps} adjoint steps (24 B/update)"}
+           "state_pool_bytes": steps * 4 * cells if every == 1 else 0,
+           "backward_note": f"backward = {recomputed} recomputed forward steps + {steps} adjoint steps "
+                            "(24 B/update: read lam, u, k and the gradient of k, write lam and the gradient)"}
     out["roofline"] = {"bound": "hbm", "achieved": out["forward_gbs"], "peak": hbm, "unit": "GB/s",
                        "frac": out["forward_gbs"] / hbm, "peak_source": src,
                        "kernel_ms": f / steps * 1e3, "algorithmic_bytes_per_launch": 12.0 * cells,
-                       "note": "forward z-walk kernel, one launch per step (read u, k; write u)"}
+                       "note": "forward staged z-walk kernel, one launch per step (read u, k; write u)"}
+    if every == 1:
+        ab = 24.0 * cells * steps / bwd / 1e9
+        out["adjoint_roofline"] = {"bound": "hbm", "achieved": ab, "peak": hbm, "unit": "GB/s", "frac": ab / hbm,
+                                   "peak_source": src, "kernel_ms": bwd / steps * 1e3,
+                                   "algorithmic_bytes_per_launch": 24.0 * cells,
+                                   "note": "adjoint step kernel; backward time / steps (the backward pass is the "
+                                           "adjoint launches only)"}
+        cf, cb, _ = run_ours(n, steps, interval=20)
+        out["checkpointed"] = {"every": 20, "forward_s": cf, "backward_s": cb,
+                               "note": f"{steps - (steps + 19) // 20} recomputed forward steps in the backward pass"}
     fh, bh, _ = run_ours(n, steps, host=True)
     out["e2e"] = {"value": cells * steps / (fh + bh) / 1e9, "unit": "GLUP/s (forward steps / forward+backward time)",
                   "h2d_bytes_per_step": 3 * 4 * cells, "d2h_bytes_per_step": 2 * 4 * cells,
@@ -1094,7 +1108,7 @@ def main():
     if rank == 0 and not args.no_batch:
         out["batched"] = batch_section(256, args.batch_steps, max(5, args.batch_steps // 50))
     if rank == 0 and not args.no_adjoint:
-        out["adjoint"] = adjoint_section(args.adjoint_n, 200, 20, 128)
+        out["adjoint"] = adjoint_section(args.adjoint_n, 200, 1, 128)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args.n, args.cpu_seconds)

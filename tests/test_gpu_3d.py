@@ -65,18 +65,21 @@ def vardiff_plain(u: xgrid.grid[float, 3], k: xgrid.grid[float, 3], dt: float) -
 
 @pytest.mark.parametrize("overstep", ["wrap", "limit"])
 @pytest.mark.parametrize("precision", ["double", "float"])
-def test_staged_and_register_zwalk_agree(cacheroot, overstep, precision):
+@pytest.mark.parametrize("shape", [(70, 35, 131), (41, 37, 132), (20, 19, 256)])
+def test_staged_and_register_zwalk_agree(cacheroot, overstep, precision, shape):
     """Mask-free 3-D grids take the staged z-walk (planes streamed through shared
     memory); the register z-walk computes the same bits, and both equal the
-    oracle.  Extents are not multiples of the staged tile (32 x 16 x 64) and span
-    several tiles; the module's count of staged launches shows which path ran."""
+    oracle.  Extents span several 8 x 128 column blocks and z chunks: rows of 131
+    cells take element copies; rows of 132 take 16-byte copies in the full block
+    and element copies in the partial one; rows of 256 are two full blocks whose
+    halo columns wrap or clamp.  The module's count of staged launches shows which
+    path ran."""
     xgrid.init(precision=precision, cacheroot=cacheroot, opt_level=3, overstep=overstep)
-    shape = (70, 35, 131)
     rng = np.random.default_rng(5)
     u0, k0 = rng.random(shape), rng.uniform(0.01, 0.1, shape)
     out = []
     for staged in (True, False):
-        k = Operator(vardiff_plain, "kernel", f"vardiff_zs_{overstep}_{precision}_{int(staged)}")
+        k = Operator(vardiff_plain, "kernel", f"vardiff_zs_{overstep}_{precision}_{shape[2]}_{int(staged)}")
         u, kk = xgrid.Grid(shape, float), xgrid.Grid(shape, float)
         u.now[...] = u0
         kk._extend_time(2)

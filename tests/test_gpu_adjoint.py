@@ -37,8 +37,10 @@ def _inputs(n, dtype, seed=4):
     return to(u0), to(kap), to(tgt), dt
 
 
-@pytest.mark.parametrize("steps,every", [(13, 5), (8, 20)])
+@pytest.mark.parametrize("steps,every", [(13, 5), (8, 20), (13, 1), (6, None)])
 def test_adjoint_matches_torch_autograd(cacheroot, steps, every):
+    """Checkpointed rollouts (every 5 steps, or one segment) and rollouts that keep
+    every state (explicitly, or by the default budget rule at this size)."""
     xgrid.init(precision="float", cacheroot=cacheroot, opt_level=3, overstep="wrap")
     k = Operator(workloads.diffuse3d.func, "kernel", "diffuse3d")
     u0, kap, tgt, dt = _inputs(20, np.float32)
@@ -120,13 +122,13 @@ def test_rollout_waits_for_inputs_made_on_the_callers_stream(cacheroot):
 
 
 @pytest.mark.parametrize("precision,dtype,tol", [("float", np.float32, 1e-5), ("double", np.float64, 1e-13)])
-def test_staged_and_register_adjoint_agree(cacheroot, precision, dtype, tol):
+@pytest.mark.parametrize("shape", [(37, 29, 70), (37, 29, 136)])
+def test_staged_and_register_adjoint_agree(cacheroot, precision, dtype, tol, shape):
     """Forward and adjoint steps through the staged z-walks (planes in shared
     memory, the default) and through the register z-walks give the same
     gradients, on extents that are not multiples of the staged column block."""
     xgrid.init(precision=precision, cacheroot=cacheroot, opt_level=3, overstep="wrap")
     rng = np.random.default_rng(9)
-    shape = (37, 29, 70)
     u0 = torch.tensor(rng.random(shape).astype(dtype), device="cuda")
     kap = torch.tensor(rng.uniform(0.01, 0.1, shape).astype(dtype), device="cuda")
     tgt = torch.tensor(rng.random(shape).astype(dtype), device="cuda")
@@ -142,3 +144,22 @@ def test_staged_and_register_adjoint_agree(cacheroot, precision, dtype, tol):
         grads.append((a.grad.clone(), b.grad.clone()))
     for g, r in zip(grads[0], grads[1]):
         assert float((g - r).abs().max() / r.abs().max()) < tol
+
+
+def test_state_budget_chooses_the_mode(cacheroot):
+    """Without an explicit interval the rollout keeps every state when the states
+    fit in the budget, else checkpoints every 20 steps; both give the same
+    gradients."""
+    xgrid.init(precision="float", cacheroot=cacheroot, opt_level=3, overstep="wrap")
+    u0, kap, tgt, dt = _inputs(16, np.float32)
+    state = u0.numel() * 4
+    out = []
+    for budget, every in ((30 * state, 1), (29 * state, 20)):
+        ro = adjoint.Rollout(Operator(workloads.diffuse3d.func, "kernel", "diffuse3d"), 30, state_budget=budget)
+        assert ro.checkpoint_interval(state) == every
+        a = u0.clone().requires_grad_(True)
+        b = kap.clone().requires_grad_(True)
+        ((ro(a, {"k": b}, (dt,)) - tgt) ** 2).mean().backward()
+        out.append((a.grad, b.grad))
+    for g, r in zip(out[0], out[1]):
+        assert float((g - r).abs().max() / r.abs().max()) < 1e-6

@@ -510,22 +510,31 @@ def build(op):
 class Rollout:
     """``steps`` forward calls of a one-sweep kernel as a differentiable map.
 
-    ``rollout = Rollout(kernel, steps, checkpoint_every=20)`` and then
-    ``u_T = rollout(u0, {"k": kappa}, (dt,))`` where ``u0`` and the coefficient
-    tensors are CUDA tensors of the grids' shape and dtype; gradients flow to
-    ``u0`` and to every coefficient tensor.  The forward pass keeps a copy of the
-    state every ``checkpoint_every`` steps; the backward pass recomputes each
-    segment from its checkpoint and runs the adjoint kernel step by step.
+    ``rollout = Rollout(kernel, steps)`` and then ``u_T = rollout(u0, {"k": kappa},
+    (dt,))`` where ``u0`` and the coefficient tensors are CUDA tensors of the grids'
+    shape and dtype; gradients flow to ``u0`` and to every coefficient tensor.
+
+    ``checkpoint_every``: ``1`` keeps every state of the forward pass (each step
+    writes straight into its slot of a state pool, so keeping them costs no
+    copies) and the backward pass runs adjoint steps only; ``k > 1`` keeps a
+    copy of the state every ``k`` steps and the backward pass recomputes each
+    segment from its checkpoint.  ``None`` (the default) keeps every state when
+    ``steps`` states fit in ``state_budget`` bytes (default: a quarter of the
+    device memory free at the forward call), else checkpoints every 20 steps.
     """
 
-    def __init__(self, kernel, steps: int, checkpoint_every: int = 20) -> None:
+    def __init__(self, kernel, steps: int, checkpoint_every: int | None = None,
+                 state_budget: int | None = None) -> None:
         from .native import NativeKernel
         if kernel.native is None:
             kernel.native = NativeKernel(kernel)
         self.kernel = kernel
         self.native = kernel.native
         self.steps = int(steps)
-        self.every = max(1, int(checkpoint_every))
+        if self.steps < 1:
+            LOG.dead("a rollout needs at least one step")
+        self.every = None if checkpoint_every is None else max(1, int(checkpoint_every))
+        self.state_budget = state_budget
         self.fn, self.meta = build(kernel)
         m = self.native.module
         self.target = m.grid_args[self.meta["target"]][0]
@@ -543,6 +552,17 @@ class Rollout:
             fn.restype = ctypes.c_int
             fn(ctypes.c_int(1 if on else 0))
 
+    def checkpoint_interval(self, state_bytes: int) -> int:
+        """Steps between kept states for states of ``state_bytes`` (1: every state)."""
+        if self.every is not None:
+            return self.every
+        budget = self.state_budget
+        if budget is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info()
+            budget = free // 4
+        return 1 if self.steps * state_bytes <= budget else 20
+
     def _grids(self, shape, dtype_type):
         from .grid import Grid
         if self.grids is None or self.grids[self.target].shape != tuple(shape):
@@ -559,6 +579,50 @@ class Rollout:
         args = self._call_args(grids, values)
         for _ in range(count):
             self.kernel(*args)
+
+    def forward_pool(self, grids, values, pool, out) -> None:
+        """Steps from ``pool[0]``: step i reads state ``pool[i]`` and writes
+        ``pool[i + 1]`` (``out`` for the last step), so every state stays without
+        copies.  The first step goes through the kernel call (ticks, uploads,
+        tables); the others call the module's entry directly with the target's two
+        level pointers moved along the pool (the coefficient grids hold the same
+        values in every level, so their levels need no rotation)."""
+        torch = _torch()
+        from . import device, runtime
+        ug = grids[self.target]
+        ug._extend_time(self.meta["depth"])
+        ug._sync_device(False)
+        own = [lv.dev for lv in ug._levels]  # the grid's own buffers, put back afterwards
+        dst = [pool[i + 1] if i + 1 < self.steps else out for i in range(self.steps)]
+        for lv, t in ((0, pool[0]), (1, dst[0])):  # after the call's tick, level 1 is the source, 0 the target
+            level = ug._levels[lv]
+            level.dev = t.view(-1).view(torch.uint8)
+            level.auth = "dev"
+        args = self._call_args(grids, values)
+        nk = self.native
+        graph, nk.use_graph = nk.use_graph, False
+        try:
+            self.kernel(*args)
+        finally:
+            nk.use_graph = graph
+            for level, buf in zip(ug._levels, own):
+                level.dev = buf
+                level.auth = "dev"
+        if self.steps == 1:
+            return
+        gl, vals = nk.split(args)
+        t = [i for i, g in enumerate(gl) if g is ug][0]
+        packed = nk.pack(vals)
+        arr = (runtime.XGGrid * len(gl))(*[g.serialize() for g in gl])
+        lib = runtime.load()
+        pargs = ctypes.cast(ctypes.byref(packed), ctypes.c_void_p) if vals else None
+        nargs = ctypes.sizeof(packed) if vals else 0
+        stream = device.stream_handle()
+        for i in range(1, self.steps):
+            arr[t].level[1] = pool[i].data_ptr()
+            arr[t].level[0] = dst[i].data_ptr()
+            if lib.xg_call(nk.fn_ptr, arr, len(gl), pargs, nargs, None, 0, stream, 0) != 0:
+                LOG.dead(f"kernel '{nk.module.name}' failed: {runtime.last_error()}")
 
     def __call__(self, u0, coefs: dict, values: tuple):
         return _RolloutFn.apply(self, tuple(values), u0, *[coefs[n] for n in self.coef_names(coefs)])
@@ -608,34 +672,43 @@ def _make_function():
             for t in (u0, *coefs):
                 t.record_stream(s)
             names = plan.coef_names(dict.fromkeys(plan.grid_names))
+            every = plan.checkpoint_interval(u0.numel() * u0.element_size())
             with torch.cuda.stream(s):
-                ftype = float
-                grids = plan._grids(u0.shape, ftype)
+                grids = plan._grids(u0.shape, float)
                 for n, t in zip(names, coefs):
                     g = grids[n]
                     g._extend_time(plan.meta["depth"])
                     for lv in range(plan.meta["depth"]):
                         g.tensor(lv).copy_(t)
-                ug = grids[plan.target]
-                ug.tensor(0).copy_(u0)
-                checkpoints = [u0.detach().clone()]
-                done = 0
-                while done < plan.steps:
-                    cnt = min(plan.every, plan.steps - done)
-                    plan.forward_steps(grids, values, cnt)
-                    done += cnt
-                    if done < plan.steps:
-                        checkpoints.append(ug.tensor(0).clone())
-                out = ug.tensor(0).clone()
+                if every == 1:
+                    # state i (before step i) in slot i; the last step writes the output
+                    dt = device.torch_dtype(grids[plan.target].numpy_dtype)
+                    pool = torch.empty((plan.steps,) + tuple(u0.shape), dtype=dt, device=u0.device)
+                    pool[0].copy_(u0)
+                    out = torch.empty_like(pool[0])
+                    plan.forward_pool(grids, values, pool, out)
+                    ctx.states = pool
+                else:
+                    ug = grids[plan.target]
+                    ug.tensor(0).copy_(u0)
+                    checkpoints = [u0.detach().clone()]
+                    done = 0
+                    while done < plan.steps:
+                        cnt = min(every, plan.steps - done)
+                        plan.forward_steps(grids, values, cnt)
+                        done += cnt
+                        if done < plan.steps:
+                            checkpoints.append(ug.tensor(0).clone())
+                    out = ug.tensor(0).clone()
+                    ctx.checkpoints = checkpoints
             _hand_back(caller, s, [out])
-            ctx.plan, ctx.values, ctx.names = plan, values, names
-            ctx.checkpoints = checkpoints
+            ctx.plan, ctx.values, ctx.names, ctx.every = plan, values, names, every
             ctx.save_for_backward(*coefs)
             return out
 
         @staticmethod
         def backward(ctx, grad_out):
-            plan, values, names = ctx.plan, ctx.values, ctx.names
+            plan, values, names, every = ctx.plan, ctx.values, ctx.names, ctx.every
             coefs = ctx.saved_tensors
             s = device.stream()
             caller = torch.cuda.current_stream()
@@ -643,40 +716,49 @@ def _make_function():
             for t in (grad_out, *coefs):
                 t.record_stream(s)
             with torch.cuda.stream(s):
-                grids = plan._grids(grad_out.shape, float)
-                ug = grids[plan.target]
                 lam = grad_out.contiguous().clone()
                 gcoef = {n: torch.zeros_like(t) for n, t in zip(names, coefs)}
                 depth, ns = plan.meta["depth"], plan.meta["nslots"]
                 packed = plan.native.pack(list(values))
                 shape3 = (ctypes.c_int64 * 3)(*([1] * (3 - lam.dim()) + list(lam.shape)))
-                for seg in reversed(range(len(ctx.checkpoints))):
-                    start = seg * plan.every
-                    cnt = min(plan.every, plan.steps - start)
-                    states = [ctx.checkpoints[seg]]
-                    ug.tensor(0).copy_(ctx.checkpoints[seg])
-                    for _ in range(cnt - 1):
-                        plan.forward_steps(grids, values, 1)
-                        states.append(ug.tensor(0).clone())
-                    for i in reversed(range(cnt)):
-                        fields = (ctypes.c_void_p * (ns * depth))()
-                        grads = (ctypes.c_void_p * ns)()
-                        for slot, n in enumerate(plan.grid_names):
-                            if n == plan.target:
-                                for lv in range(depth):
-                                    fields[slot * depth + lv] = states[i].data_ptr()
-                            else:
-                                t = coefs[names.index(n)]
-                                for lv in range(depth):
-                                    fields[slot * depth + lv] = t.data_ptr()
-                                grads[slot] = gcoef[n].data_ptr()
-                        new = torch.empty_like(lam)
-                        rc = plan.fn(new.data_ptr(), lam.data_ptr(), fields, grads, shape3,
-                                     ctypes.byref(packed) if plan.value_names else None,
-                                     ctypes.sizeof(packed) if plan.value_names else 0, device.stream_handle())
-                        if rc != 0:
-                            LOG.dead(f"adjoint kernel failed: {runtime.last_error()}")
-                        lam = new
+
+                def adjoint_step(state):
+                    fields = (ctypes.c_void_p * (ns * depth))()
+                    grads = (ctypes.c_void_p * ns)()
+                    for slot, n in enumerate(plan.grid_names):
+                        if n == plan.target:
+                            for lv in range(depth):
+                                fields[slot * depth + lv] = state.data_ptr()
+                        else:
+                            t = coefs[names.index(n)]
+                            for lv in range(depth):
+                                fields[slot * depth + lv] = t.data_ptr()
+                            grads[slot] = gcoef[n].data_ptr()
+                    new = torch.empty_like(lam)
+                    rc = plan.fn(new.data_ptr(), lam.data_ptr(), fields, grads, shape3,
+                                 ctypes.byref(packed) if plan.value_names else None,
+                                 ctypes.sizeof(packed) if plan.value_names else 0, device.stream_handle())
+                    if rc != 0:
+                        LOG.dead(f"adjoint kernel failed: {runtime.last_error()}")
+                    return new
+
+                if every == 1:
+                    for i in reversed(range(plan.steps)):
+                        lam = adjoint_step(ctx.states[i])
+                    ctx.states = None
+                else:
+                    grids = plan._grids(grad_out.shape, float)
+                    ug = grids[plan.target]
+                    for seg in reversed(range(len(ctx.checkpoints))):
+                        start = seg * every
+                        cnt = min(every, plan.steps - start)
+                        states = [ctx.checkpoints[seg]]
+                        ug.tensor(0).copy_(ctx.checkpoints[seg])
+                        for _ in range(cnt - 1):
+                            plan.forward_steps(grids, values, 1)
+                            states.append(ug.tensor(0).clone())
+                        for i in reversed(range(cnt)):
+                            lam = adjoint_step(states[i])
             _hand_back(caller, s, [lam] + list(gcoef.values()))
             return (None, None, lam) + tuple(gcoef[n] for n in names)
 

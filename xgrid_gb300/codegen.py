@@ -49,9 +49,11 @@ ZWALK_BLOCKS = 4
 
 # staged z-walk of mask-free 3-D sweeps: (y, x) column block of a CTA, thread rows, planes
 # prefetched beyond the next one (chunk lengths along z: xg_zstage_chunks)
-ZSTAGE_TILE = (16, 64)
+ZSTAGE_TILE = (8, 128)
 ZSTAGE_THREADS = 256
-ZSTAGE_AHEAD = 2
+ZSTAGE_AHEAD = 1
+ZSTAGE_AHEAD_WIDE = 1  # with three or more staged buffers (three CTAs per SM still fit)
+ZSTAGE_MAX_BLOCKS = 3
 
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
 DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 64, 32, 32, 8, 1), 3: (64, 4, 64, 64, 4, 1)}
@@ -911,12 +913,13 @@ def zstage_geometry(T: str, nb: int) -> dict:
     v = 16 // size
     ntx = tx // v
     nty = ZSTAGE_THREADS // ntx
-    d = ZSTAGE_AHEAD if nb <= 2 else 1
+    assert nty >= 1 and ty % nty == 0, "staged tile rows must be a multiple of the thread rows"
+    d = ZSTAGE_AHEAD if nb <= 2 else ZSTAGE_AHEAD_WIDE
     px = tx + 2 * v
     smem = (d + 3) * nb * (ty + 2) * px * size
-    # CTAs per SM that the shared memory allows (228 KiB per SM, 1 KiB reserved per CTA), at most 3:
-    # the register budget ptxas gets follows from it
-    blocks = max(1, min(3, (228 * 1024) // (smem + 1024)))
+    # CTAs per SM that the shared memory allows (228 KiB per SM, 1 KiB reserved per CTA), at most
+    # ZSTAGE_MAX_BLOCKS: the register budget ptxas gets follows from it
+    blocks = max(1, min(ZSTAGE_MAX_BLOCKS, (228 * 1024) // (smem + 1024)))
     return {"V": v, "NTX": ntx, "NTY": nty, "RY": ty // nty, "D": d, "PX": px, "TY": ty, "TX": tx,
             "smem": smem, "size": size, "blocks": blocks}
 
@@ -948,7 +951,7 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
          f"{kname}(const __grid_constant__ {ptype} p, const int zlen, const int vec) {{",
          f"  constexpr int TY = {TY}, TX = {TX}, V = {V}, NTX = {NTX}, NT = {ZSTAGE_THREADS}, D = {D};",
          f"  constexpr int PX = {PX}, PY = TY + 2, PL = PY * PX, R = D + 3, NB = {nb};",
-         "  constexpr int KV = (PL / V + NT - 1) / NT, KE = (PL + NT - 1) / NT;",
+         "  constexpr int CR = TX / V + 2, KC = (PY * CR + NT - 1) / NT;  // copies per row and per thread",
          "  extern __shared__ __align__(16) unsigned char xg_zs_raw[];",
          f"  {T}* const ring = ({T}*)xg_zs_raw;  // [R][NB][PY][PX]",
          "  const int tid = threadIdx.x;",
@@ -957,24 +960,26 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
          "  const int x0 = ix * TX, y0 = iy * TY, z0 = iz * zlen;",
          "  const int z1 = z0 + zlen < (int)p.Z ? z0 + zlen : (int)p.Z;",
          "  const I sy = (I)p.X, sz = (I)(p.X * p.Y);",
-         "  // 16-byte staging: the rows x0 - V .. x0 + TX + V - 1 lie inside the grid",
-         "  const bool vst = vec && x0 >= V && x0 + TX + V <= (int)p.X;",
-         "  // this thread's staging copies: their (wrapped or clamped) element offsets in a plane, -1 = none",
-         "  I goff[KE];",
+         "  // a full block of 16-byte aligned rows: each staged row is TX / V 16-byte copies of the",
+         "  // block's cells and two element copies of its halo cells (wrapped or clamped)",
+         "  const bool vst = vec && x0 + TX <= (int)p.X;",
+         "  I goff[KC];",
+         "  int soff[KC];  // ring offset of a 16-byte copy, or -2 - offset of an element copy, -1: none",
          "#pragma unroll",
-         "  for (int k = 0; k < KE; ++k) {",
-         "    const int e = tid + k * NT;",
-         "    goff[k] = -1;",
-         "    if (vst) {",
-         "      if (k < KV && e < PL / V) {",
-         "        const int r = (e * V) / PX, c = (e * V) % PX;",
-         "        goff[k] = (I)xg_axis(xg_overstep, y0 - 1 + r, (int)p.Y) * sy + (I)(x0 - V + c);",
+         "  for (int k = 0; k < KC; ++k) {",
+         "    const int e = tid + k * NT, r = e / CR, j = e % CR;",
+         "    soff[k] = -1;",
+         "    goff[k] = 0;",
+         "    if (vst && r < PY) {",
+         "      const I row = (I)xg_axis(xg_overstep, y0 - 1 + r, (int)p.Y) * sy;",
+         "      if (j < TX / V) {",
+         "        soff[k] = r * PX + V + j * V;",
+         "        goff[k] = row + x0 + j * V;",
+         "      } else {",
+         "        const int left = j == TX / V;",
+         "        soff[k] = -2 - (r * PX + (left ? V - 1 : V + TX));",
+         "        goff[k] = row + (I)xg_axis(xg_overstep, left ? x0 - 1 : x0 + TX, (int)p.X);",
          "      }",
-         "    } else if (e < PL) {",
-         "      const int r = e / PX, c = e % PX;",
-         "      if (c >= V - 1 && c <= V + TX)",
-         "        goff[k] = (I)xg_axis(xg_overstep, y0 - 1 + r, (int)p.Y) * sy + "
-         "(I)xg_axis(xg_overstep, x0 - V + c, (int)p.X);",
          "    }",
          "  }",
          f"  const {T}* const src[NB] = {{{', '.join(srcs)}}};",
@@ -986,14 +991,18 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
          "#pragma unroll",
          "        for (int b = 0; b < NB; ++b)",
          "#pragma unroll",
-         "          for (int k = 0; k < KV; ++k)",
-         "            if (goff[k] >= 0) xg_cp_async16(slot + b * PL + (tid + k * NT) * V, src[b] + zb + goff[k]);",
-         "      } else {",
+         "          for (int k = 0; k < KC; ++k) {",
+         "            if (soff[k] >= 0) xg_cp_async16(slot + b * PL + soff[k], src[b] + zb + goff[k]);",
+         "            else if (soff[k] < -1) xg_cp_async(slot + b * PL + (-2 - soff[k]), src[b] + zb + goff[k]);",
+         "          }",
+         "      } else {  // element copies of columns V - 1 .. V + TX of every row",
+         "        for (int e = tid; e < PY * (TX + 2); e += NT) {",
+         "          const int r = e / (TX + 2), c = e % (TX + 2);",
+         "          const I off = (I)xg_axis(xg_overstep, y0 - 1 + r, (int)p.Y) * sy + "
+         "(I)xg_axis(xg_overstep, x0 - 1 + c, (int)p.X);",
          "#pragma unroll",
-         "        for (int b = 0; b < NB; ++b)",
-         "#pragma unroll",
-         "          for (int k = 0; k < KE; ++k)",
-         "            if (goff[k] >= 0) xg_cp_async(slot + b * PL + tid + k * NT, src[b] + zb + goff[k]);",
+         "          for (int b = 0; b < NB; ++b) xg_cp_async(slot + b * PL + r * PX + V - 1 + c, src[b] + zb + off);",
+         "        }",
          "      }",
          "    }",
          "    xg_cp_async_commit();",
