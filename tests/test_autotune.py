@@ -24,21 +24,20 @@ def test_group_candidates_are_valid_launches(ndim):
 @pytest.mark.parametrize("shape", [(1025, 1025), (2049, 2049), (513, 1537), (4097, 4097)])
 @pytest.mark.parametrize("sms", [152, 148, 132])
 def test_balanced_candidates_fill_whole_waves(shape, sms):
+    """Every candidate's tile count (rows of tiles given as a count, columns of tx
+    cells) is exactly k waves of 3, 4 or 6 resident CTAs per SM."""
     Y, X = shape
     cands = autotune.balanced_candidates(shape, sms)
     assert cands, "no balanced candidate"
     for tz, ty, tx, bx, by, bz in cands:
-        assert (tz, bx, by, bz) == (1, 32, 8, 1) and 8 <= ty <= 256
-        full = (Y // ty) * (X // tx)
-        # every full tile in one of k waves of 4 or 6 resident CTAs per SM, within rounding
-        # of the tile height (one row of tiles)
-        waves = [full / (k * sms * per) for per in (4, 6) for k in (1, 2, 3)]
-        assert any(0.8 <= w <= 1.0 + 1e-9 for w in waves), (ty, tx, full, waves)
+        assert tz == 1 and bz == 1 and (bx, by) in ((32, 8), (64, 4)) and ty < 0 and tx >= bx
+        count = (-ty) * (X // tx)
+        assert count in {k * sms * per for per in (3, 4, 6) for k in (1, 2)}, (ty, tx, count)
 
 
 def test_balanced_candidates_for_1025_fill_152_sms():
-    # the 1025^2 cavity on 152 SMs x 4 CTAs: 54-row tiles give 19 x 32 = 608 full tiles
-    assert (1, 54, 32, 32, 8, 1) in autotune.balanced_candidates((1025, 1025), 152)
+    # the 1025^2 cavity on 152 SMs x 4 CTAs: 76 rows of 128-column tiles = 608 tiles
+    assert (1, -76, 128, 32, 8, 1) in autotune.balanced_candidates((1025, 1025), 152)
     assert autotune.balanced_candidates((1025, 1025, 3), 152) == []
     assert autotune.balanced_candidates((64, 64), 152) == []
 

@@ -77,3 +77,29 @@ def test_tuned_batch_equals_default_batch(cacheroot):
     k2.batch(b, 24, temporal=1)
     for pa, pb in zip(a, b):
         assert pa[0].read(0).tobytes() == pb[0].read(0).tobytes()
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+@pytest.mark.parametrize("tiling", [(1, -76, 128, 32, 8, 1), (1, -7, 64, 64, 4, 1), (1, -257, 32, 32, 8, 1),
+                                    (1, 27, 64, 32, 8, 1)])
+def test_even_tile_rows_keep_the_bits(cacheroot, tiling, persistent):
+    """A tiling moves work between CTAs only: rows of tiles split evenly (given as a
+    count, e.g. 76 rows of 3 or 4 cells on 257 rows, or as a least height) and
+    columns of tx cells give the default tiling's bits in every level, for fused
+    groups and for persistent loop launches."""
+    n = 257
+    xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3, persistent=persistent)
+    tiled = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
+    plain = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
+    ga, cfg = workloads.cavity_setup(n, 1e-5, seed=3)
+    gb, _ = workloads.cavity_setup(n, 1e-5, seed=3)
+    a = (ga["b"], ga["p"], ga["u"], ga["v"], cfg)
+    b = (gb["b"], gb["p"], gb["u"], gb["v"], cfg)
+    tiled(*a)
+    plain(*b)
+    for g in range(tiled.native.module.groups):
+        tiled.native.set_tiling(g, tiling)
+    for _ in range(4):
+        tiled(*a)
+        plain(*b)
+    assert _state(ga) == _state(gb)

@@ -168,23 +168,32 @@ def tune_batch(native, problems, candidates=None) -> tuple:
 
 # ------------------------------------------------------------ single calls
 def balanced_candidates(shape, sms: int) -> list:
-    """2-D tilings whose number of full tiles is a whole number of waves: k x SMs x
-    (4 or 6 resident CTAs per SM, the FP64 and FP32 tile kernels' occupancies).
-    Power-of-two tiles of a 2^n + 1 grid give 2^m full tiles, which never fill
-    152 x 4 slots (1025^2 with 64 x 32 tiles: 512 tiles, 84 % of one wave)."""
+    """2-D tilings whose tile count is a whole number of waves, k x SMs x (3, 4 or 6
+    resident CTAs per SM, the tile kernels' occupancies), with tiles of equal work:
+    x tiles of 32 to 256 columns (the last one absorbs the remainder, a column or
+    two on 2^n + 1 grids) and a tile count along y given directly (a negative ty),
+    y being split evenly.  Power-of-two tiles of a 2^n + 1 grid give 2^m tiles,
+    which never fill 152 x 4 slots (1025^2 with 64 x 32 tiles: 512 tiles, 84 % of
+    one wave)."""
     if len(shape) != 2 or sms <= 0:
         return []
     Y, X = shape
     out = []
-    for per_sm in (4, 6):
-        for tx in (32, 64):
-            nx = max(1, X // tx)
-            for k in (1, 2, 3):
-                nty = max(1, (k * sms * per_sm) // nx)
-                ty = -(-Y // nty)
-                c = (1, ty, tx, 32, 8, 1)
-                if 8 <= ty <= 256 and c not in out:
-                    out.append(c)
+    for per_sm in (3, 4, 6):
+        for tx in (32, 64, 128, 256):
+            nx = X // tx
+            if nx < 1:
+                continue
+            for k in (1, 2):
+                target = k * sms * per_sm
+                if target % nx or not 1 <= target // nx <= Y:
+                    continue
+                for block in ((32, 8, 1), (64, 4, 1)):
+                    if block[0] > tx:
+                        continue
+                    c = (1, -(target // nx), tx, *block)
+                    if c not in out:
+                        out.append(c)
     return out
 
 

@@ -309,9 +309,8 @@ class BatchEmitter:
              "    const int t = (int)(it - D.tile0);  // a problem has fewer than 2^31 tiles",
              "    const int ntx = (int)p.ntx, nty = (int)p.nty, ntz = (int)p.ntz;",
              "    const int itx = t % ntx, trow = t / ntx, ity = trow % nty, itz = trow / nty;",
-             "    const int x0 = itx * p.tx, x1 = itx == ntx - 1 ? (int)p.X : (itx + 1) * p.tx;",
-             "    const int y0 = ity * p.ty, y1 = ity == nty - 1 ? (int)p.Y : (ity + 1) * p.ty;",
-             "    const int z0 = itz * p.tz, z1 = itz == ntz - 1 ? (int)p.Z : (itz + 1) * p.tz;",
+             "    const xg_tile T_ = xg_tile_even(itz, ity, itx, p.Z, p.Y, p.X, p.tx, nty, ntx, ntz);",
+             "    const int x0 = T_.x0, x1 = T_.x1, y0 = T_.y0, y1 = T_.y1, z0 = T_.z0, z1 = T_.z1;",
              "    const I sy = (I)p.X, sz = (I)(p.X * p.Y);",
              "    (void)sy; (void)sz;"]
         for b in e.buffers(g.sweeps):

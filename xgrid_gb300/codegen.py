@@ -54,6 +54,8 @@ ZSTAGE_THREADS = 256
 ZSTAGE_AHEAD = 1
 ZSTAGE_AHEAD_WIDE = 1  # with three or more staged buffers (three CTAs per SM still fit)
 ZSTAGE_MAX_BLOCKS = 3
+ZSTAGE_SHUFFLE = False
+ZSTAGE_ONE_BARRIER = True
 
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
 DEFAULT_TILING = {1: (1, 1, 1024, 256, 1, 1), 2: (1, 64, 32, 32, 8, 1), 3: (64, 4, 64, 64, 4, 1)}
@@ -916,12 +918,17 @@ def zstage_geometry(T: str, nb: int) -> dict:
     assert nty >= 1 and ty % nty == 0, "staged tile rows must be a multiple of the thread rows"
     d = ZSTAGE_AHEAD if nb <= 2 else ZSTAGE_AHEAD_WIDE
     px = tx + 2 * v
-    smem = (d + 3) * nb * (ty + 2) * px * size
-    # CTAs per SM that the shared memory allows (228 KiB per SM, 1 KiB reserved per CTA), at most
-    # ZSTAGE_MAX_BLOCKS: the register budget ptxas gets follows from it
-    blocks = max(1, min(ZSTAGE_MAX_BLOCKS, (228 * 1024) // (smem + 1024)))
+    plane = nb * (ty + 2) * px * size
+
+    def fit(slots):
+        # CTAs per SM that the shared memory allows (228 KiB per SM, 1 KiB reserved per CTA), at
+        # most ZSTAGE_MAX_BLOCKS: the register budget ptxas gets follows from it
+        return max(1, min(ZSTAGE_MAX_BLOCKS, (228 * 1024) // (slots * plane + 1024)))
+    # D + 3 slots: planes z - 1, z, z + 1 and D in flight, a second barrier per plane before a
+    # slot is refilled; one slot more lets the plane's first barrier cover the refill
+    slots = d + 4 if ZSTAGE_ONE_BARRIER and fit(d + 4) == fit(d + 3) else d + 3
     return {"V": v, "NTX": ntx, "NTY": nty, "RY": ty // nty, "D": d, "PX": px, "TY": ty, "TX": tx,
-            "smem": smem, "size": size, "blocks": blocks}
+            "R": slots, "smem": slots * plane, "size": size, "blocks": fit(slots)}
 
 
 def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: list) -> str:
@@ -943,14 +950,17 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
     destination's value when ``accumulate``; a guard skips the output when it
     is null.  The parameter struct has Z, Y, X."""
     g = zstage_geometry(T, len(srcs))
-    V, NTX, NTY, RY, D, PX, TY, TX = (g[k] for k in ("V", "NTX", "NTY", "RY", "D", "PX", "TY", "TX"))
+    V, NTX, NTY, RY, D, PX, TY, TX, R = (g[k] for k in ("V", "NTX", "NTY", "RY", "D", "PX", "TY", "TX", "R"))
+    # x-neighbours from the adjacent lanes when a warp covers whole rows (measured slower than
+    # reading them from the ring: the shuffle waits for the vector load)
+    shuffle = ZSTAGE_SHUFFLE and NTX % 32 == 0
     VT = "double2" if T == "double" else "float4"
     nb = len(srcs)
     comp = "xyzw"
     K = [f"template <typename I> __global__ void __launch_bounds__({ZSTAGE_THREADS}, {g['blocks']}) "
          f"{kname}(const __grid_constant__ {ptype} p, const int zlen, const int vec) {{",
          f"  constexpr int TY = {TY}, TX = {TX}, V = {V}, NTX = {NTX}, NT = {ZSTAGE_THREADS}, D = {D};",
-         f"  constexpr int PX = {PX}, PY = TY + 2, PL = PY * PX, R = D + 3, NB = {nb};",
+         f"  constexpr int PX = {PX}, PY = TY + 2, PL = PY * PX, R = {R}, NB = {nb};",
          "  constexpr int CR = TX / V + 2, KC = (PY * CR + NT - 1) / NT;  // copies per row and per thread",
          "  extern __shared__ __align__(16) unsigned char xg_zs_raw[];",
          f"  {T}* const ring = ({T}*)xg_zs_raw;  // [R][NB][PY][PX]",
@@ -1008,12 +1018,13 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
          "    xg_cp_async_commit();",
          "  };",
          "#pragma unroll",
-         "  for (int q = 0; q < R - 1; ++q) stage(z0 - 1 + q);",
+         "  for (int q = 0; q < D + 2; ++q) stage(z0 - 1 + q);  // planes z0 - 1 .. z0 + D",
          "  const int tx_t = tid % NTX, ty_t = tid / NTX;",
          "  const int c0 = V + V * tx_t, x = x0 + V * tx_t;  // the thread's first cell: ring column, grid x",
          "  XG_ZSTAGE_WINDOW",
          "  for (int z = z0; z < z1; ++z) {",
-         "    stage(z + D + 1);  // into the slot plane z - 2 used (freed by the barrier below)",
+         "    stage(z + D + 1);  // into the slot of plane z + D + 2 - R, read for the last time before the",
+         "                       // previous plane's first barrier (R = D + 4) or its second (R = D + 3)",
          "    xg_cp_async_wait_group<D>();  // planes up to z + 1 have landed",
          "    __syncthreads();",
          f"    const {T}* const pl_m = ring + ((z - z0) % R) * NB * PL;      // plane z - 1",
@@ -1023,7 +1034,7 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
          "#pragma unroll",
          f"    for (int i = 0; i < {RY}; ++i) {{",
          f"      const int r = ty_t + i * {NTY} + 1, y = y0 + r - 1;",
-         "      if (y < (int)p.Y && x < (int)p.X) {",
+         "      if (y < (int)p.Y) {  // the same for every lane of a warp that covers whole rows",
          "        const I gb = (I)z * sz + (I)y * sy + (I)x;"]
     # rows of the ring this thread reads: (buffer, oz, oy) -> which of x-1 / x+V it needs too
     rows = {}
@@ -1051,9 +1062,16 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
             K.append(f"        const {VT} {w} = zw{b}_{'m' if oz < 0 else 'c'}[i];")
         else:
             K.append(f"        const {VT} {w} = *reinterpret_cast<const {VT}*>(&{base}]);")
-        if -1 in oxs:
+        last = comp[V - 1]
+        if -1 in oxs and shuffle:
+            K.append(f"        const {T} {w}_ls = __shfl_up_sync(0xffffffffu, {w}.{last}, 1);")
+            K.append(f"        const {T} {w}_l = (tx_t & 31) == 0 ? {base} - 1] : {w}_ls;")
+        elif -1 in oxs:
             K.append(f"        const {T} {w}_l = {base} - 1];")
-        if 1 in oxs:
+        if 1 in oxs and shuffle:
+            K.append(f"        const {T} {w}_rs = __shfl_down_sync(0xffffffffu, {w}.x, 1);")
+            K.append(f"        const {T} {w}_r = (tx_t & 31) == 31 ? {base} + V] : {w}_rs;")
+        elif 1 in oxs:
             K.append(f"        const {T} {w}_r = {base} + V];")
     for o, _ in enumerate(outs):
         K.append(f"        {T} o{o}[V];")
@@ -1069,6 +1087,7 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
         for o, (_, value, _, _) in enumerate(outs):
             K.append(f"          o{o}[{j}] = {value};")
         K.append("        }")
+    K.append("        if (x < (int)p.X) {")
     K.append("        if (vec) {  // one 16-byte store per output")
     for o, (dst, _, guard, acc) in enumerate(outs):
         ind = "          "
@@ -1093,13 +1112,15 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
         else:
             K.append(f"              {pre}{dst}[gb + j] = o{o}[j];")
     K += ["            }",
+          "        }",
           "        }"]
     for b in zw:
         K += [f"        zw{b}_m[i] = zw{b}_c[i];", f"        zw{b}_c[i] = {rn(b, 1, 0)};"]
     K += ["      }",
-          "    }",
-          "    __syncthreads();  // the slot of plane z - 1 is free for plane z + D + 2",
-          "  }",
+          "    }"]
+    if R == D + 3:
+        K.append("    __syncthreads();  // the slot of plane z - 1 is refilled at the next plane")
+    K += ["  }",
           "  xg_cp_async_wait_all();",
           "}"]
     decl = " ".join(f"{VT} zw{b}_m[{RY}], zw{b}_c[{RY}];" for b in zw)

@@ -248,7 +248,11 @@ __device__ __forceinline__ void xg_tile_range(int64_t n, int32_t t, int64_t nt, 
   *hi = (i == nt - 1) ? n : (i + 1) * t;
 }
 
-static inline int64_t xg_tiles_along(int64_t n, int32_t t) { return n / t > 0 ? n / t : 1; }
+// Tiles along an axis of n cells for tiles of at least t cells, or -t tiles when t is
+// negative (z and y only; xg_tile_of has the rule).
+static inline int64_t xg_tiles_along(int64_t n, int32_t t) {
+  return t < 0 ? (n < -(int64_t)t ? n : -(int64_t)t) : (n / t > 0 ? n / t : 1);
+}
 
 // The tile of the calling CTA: the launch grid is (ntx, nty, ntz) tiles, so the
 // tile coordinates are the block indices (no division); t is the linear tile id
@@ -258,18 +262,26 @@ struct xg_tile {
   int64_t t;
 };
 
+// Tile (iz, iy, ix): along z and y, tile i of nt covers [i * n / nt, (i + 1) * n / nt)
+// (even split, tiles differ by at most one cell); along x, tiles of tx cells with the
+// last one absorbing the remainder (columns stay aligned to the warps).
+__device__ __forceinline__ xg_tile xg_tile_even(int64_t iz, int64_t iy, int64_t ix, int64_t Z, int64_t Y, int64_t X,
+                                                int tx, int64_t nty, int64_t ntx, int64_t ntz) {
+  xg_tile T;
+  T.t = (iz * nty + iy) * ntx + ix;
+  T.x0 = (int)(ix * tx);
+  T.x1 = (ix == ntx - 1) ? (int)X : (int)((ix + 1) * tx);
+  T.y0 = (int)(iy * Y / nty);
+  T.y1 = (int)((iy + 1) * Y / nty);
+  T.z0 = (int)(iz * Z / ntz);
+  T.z1 = (int)((iz + 1) * Z / ntz);
+  return T;
+}
+
 __device__ __forceinline__ xg_tile xg_tile_of(int64_t Z, int64_t Y, int64_t X, int tz, int ty, int tx,
                                               int64_t nty, int64_t ntx, int64_t ntz) {
-  xg_tile T;
-  const int ix = blockIdx.x, iy = blockIdx.y, iz = blockIdx.z;
-  T.t = ((int64_t)iz * nty + iy) * ntx + ix;
-  T.x0 = ix * tx;
-  T.x1 = (ix == ntx - 1) ? (int)X : (ix + 1) * tx;
-  T.y0 = iy * ty;
-  T.y1 = (iy == nty - 1) ? (int)Y : (iy + 1) * ty;
-  T.z0 = iz * tz;
-  T.z1 = (iz == ntz - 1) ? (int)Z : (iz + 1) * tz;
-  return T;
+  (void)tz; (void)ty;
+  return xg_tile_even(blockIdx.z, blockIdx.y, blockIdx.x, Z, Y, X, tx, nty, ntx, ntz);
 }
 
 // Tile kernels are instantiated for int and int64_t linear indices; the 32-bit
@@ -398,16 +410,8 @@ __device__ __forceinline__ bool xg_mbar_wait(uint64_t* bar, unsigned parity, uin
 // Tile number t of a (ntz, nty, ntx) tiling, numbered like xg_tile_of.
 __device__ __forceinline__ xg_tile xg_tile_at(int64_t t, int64_t Z, int64_t Y, int64_t X, int tz, int ty, int tx,
                                               int64_t nty, int64_t ntx, int64_t ntz) {
-  xg_tile T;
-  const int ix = (int)(t % ntx), iy = (int)((t / ntx) % nty), iz = (int)(t / (ntx * nty));
-  T.t = t;
-  T.x0 = ix * tx;
-  T.x1 = (ix == ntx - 1) ? (int)X : (ix + 1) * tx;
-  T.y0 = iy * ty;
-  T.y1 = (iy == nty - 1) ? (int)Y : (iy + 1) * ty;
-  T.z0 = iz * tz;
-  T.z1 = (iz == ntz - 1) ? (int)Z : (iz + 1) * tz;
-  return T;
+  (void)tz; (void)ty;
+  return xg_tile_even(t / (ntx * nty), (t / ntx) % nty, t % ntx, Z, Y, X, tx, nty, ntx, ntz);
 }
 
 // Completion flags of a persistent loop launch: flags[t] counts the iterations

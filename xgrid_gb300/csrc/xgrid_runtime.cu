@@ -143,14 +143,26 @@ struct xg_mask {
 
 namespace {
 
-inline int64_t tile_count(int64_t n, int32_t t) { return std::max<int64_t>(1, n / t); }
-inline int64_t tile_of(int64_t c, int32_t t, int64_t nt) { return std::min<int64_t>(c / t, nt - 1); }
+// Tilings (tz, ty, tx), the rule xg_tile_of in the generated code follows: the z and y
+// axes are split evenly into nt = max(1, n / t) tiles -- or into -t tiles when t is
+// negative -- tile i covering [i * n / nt, (i + 1) * n / nt), so their tiles differ by
+// at most one cell; the x axis has tiles of tx cells, the last one absorbing the
+// remainder, so that tile columns stay aligned to the warps that sweep them.
+inline int64_t tile_count(int64_t n, int32_t t) {
+  return t < 0 ? std::min<int64_t>(n, -(int64_t)t) : std::max<int64_t>(1, n / t);
+}
+inline int64_t tile_of_even(int64_t c, int64_t n, int64_t nt) { return ((c + 1) * nt - 1) / n; }
+inline int64_t tile_of_last(int64_t c, int32_t t, int64_t nt) { return std::min<int64_t>(c / t, nt - 1); }
+// shortest tile along an axis
+inline int64_t tile_min(int axis, int64_t n, int32_t t, int64_t nt) { return axis == 2 ? (nt > 1 ? t : n) : n / nt; }
+inline bool tiling_valid(const int32_t* t) { return t[0] != 0 && t[1] != 0 && t[2] >= 1; }
 
 int64_t tile_id(const xg_mask* m, const Tiles& T, const TileKey& k, int64_t lin) {
   int64_t x = lin % m->ext[2];
   int64_t y = (lin / m->ext[2]) % m->ext[1];
   int64_t z = lin / (m->ext[2] * m->ext[1]);
-  int64_t iz = tile_of(z, k.tz, T.nt[0]), iy = tile_of(y, k.ty, T.nt[1]), ix = tile_of(x, k.tx, T.nt[2]);
+  int64_t iz = tile_of_even(z, m->ext[0], T.nt[0]), iy = tile_of_even(y, m->ext[1], T.nt[1]),
+          ix = tile_of_last(x, k.tx, T.nt[2]);
   return (iz * T.nt[1] + iy) * T.nt[2] + ix;
 }
 
@@ -324,7 +336,7 @@ int xg_mask_nonzero(const xg_mask* m, int64_t* count) {
 int xg_mask_tiles(xg_mask* m, const int32_t* tile, int32_t value, const uint8_t** tile_zero,
                   const int32_t** csr_off, const int64_t** csr_cells, int64_t* ntiles) {
   if (!m || !tile) return fail("xg_mask_tiles: null argument");
-  if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1) return fail("xg_mask_tiles: tile extents must be positive");
+  if (!tiling_valid(tile)) return fail("xg_mask_tiles: tile extents must be nonzero (x positive)");
   TileKey key{tile[0], tile[1], tile[2]};
   auto it = m->tiles.find(key);
   if (it == m->tiles.end()) {
@@ -407,14 +419,14 @@ int xg_mask_tile_reach(xg_mask* m, const int32_t* tile, int noff, const int32_t*
   const int32_t ext[3] = {tile[0], tile[1], tile[2]};
   int64_t nt[3], reach[3] = {0, 0, 0};
   for (int a = 0; a < 3; ++a) {
-    if (ext[a] < 1) return fail("xg_mask_tile_reach: tile extents must be positive");
+    if (!tiling_valid(ext)) return fail("xg_mask_tile_reach: tile extents must be nonzero (x positive)");
     nt[a] = tile_count(m->ext[a], ext[a]);
     for (int k = 0; k < noff; ++k) reach[a] = std::max<int64_t>(reach[a], std::abs(offsets[3 * k + a]));
   }
-  // a read may reach the next tile along an axis, never the one after it (the last
-  // tile of an axis absorbs the remainder, so it is at least as long as the others)
+  // a read may reach the next tile along an axis, never the one after it: the reach
+  // must not exceed the shortest tile
   for (int a = 0; a < 3; ++a)
-    if (nt[a] > 1 && reach[a] > ext[a]) {
+    if (nt[a] > 1 && reach[a] > tile_min(a, m->ext[a], ext[a], nt[a])) {
       *ok = 0;
       return 0;
     }
@@ -437,9 +449,9 @@ int xg_mask_tile_reach(xg_mask* m, const int32_t* tile, int noff, const int32_t*
   const int64_t X = m->ext[2], Y = m->ext[1], Z = m->ext[0];
   auto tile_of3 = [&](int64_t lin, int64_t* c) {
     const int64_t x = lin % X, y = (lin / X) % Y, z = lin / (X * Y);
-    c[0] = tile_of(z, ext[0], nt[0]);
-    c[1] = tile_of(y, ext[1], nt[1]);
-    c[2] = tile_of(x, ext[2], nt[2]);
+    c[0] = tile_of_even(z, Z, nt[0]);
+    c[1] = tile_of_even(y, Y, nt[1]);
+    c[2] = tile_of_last(x, ext[2], nt[2]);
   };
   for (int64_t z = 0; z < Z && result; ++z)
     for (int64_t y = 0; y < Y && result; ++y) {
