@@ -138,10 +138,16 @@ def kernels_only(args) -> None:
     xgrid.init(precision="double", cacheroot=JIT_CACHE,
                opt_level=3, mixed=args.mixed, mixed_temporal=args.mixed_temporal, persistent=bool(args.persistent))
     grids, cfg = workloads.cavity_setup(args.n, stable_dt(args.n))
+    args_ = (grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+    tilings = None
+    if not args.no_tune and args.mixed is None:
+        # the bench's tile choice (timed on these grids, cached on disk per shape)
+        from xgrid_gb300 import autotune
+        tilings = {str(g): list(t) for g, t in autotune.tune(workloads.cavity_kernel, *args_).items()}
     for _ in range(args.warmup + args.steps):
-        workloads.cavity_kernel(grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+        workloads.cavity_kernel(*args_)
     device.synchronize()
-    print(json.dumps({"mode": "kernels", "n": args.n, "calls": args.warmup + args.steps}))
+    print(json.dumps({"mode": "kernels", "n": args.n, "calls": args.warmup + args.steps, "tilings": tilings}))
 
 
 def peaks():
@@ -153,24 +159,23 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel_tag: str, n: int):
-    """DRAM bytes (read + write) per launch of the dominant kernel, from the
-    committed ncu summaries (``traffic_bytes_per_launch_<n>: <bytes>`` lines in
-    ``profiles/<kernel_tag>_*.md``).  A capture at another size is scaled by the
-    number of cells (the kernel's traffic is proportional to its cells); None
-    when no capture exists."""
+def profile_traffic(kernel_tag: str, n: int, key: str = "traffic_bytes_per_launch_", dims: int = 2):
+    """DRAM bytes (read + write) per launch of a kernel, from the committed ncu
+    summaries (``<key><n>: <bytes>`` lines in ``profiles/<kernel_tag>_*.md``).
+    A capture at another size is scaled by the number of cells (n^dims; the
+    kernel's traffic is proportional to its cells); None when no capture exists."""
     import glob
     found = {}
     for path in glob.glob(os.path.join(ROOT, "profiles", f"{kernel_tag}_*.md")):
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch_"):
-                key, val = line.split(":", 1)
-                found[int(key.rsplit("_", 1)[1])] = float(val)
+            if line.startswith(key):
+                k, val = line.split(":", 1)
+                found[int(k[len(key):])] = float(val)
     if n in found:
-        return found[n], f"ncu capture at {n}^2"
+        return found[n], f"ncu capture at {n}^{dims}"
     if found:
         m = max(found)
-        return found[m] * (n * n) / (m * m), f"ncu capture at {m}^2 scaled by cells"
+        return found[m] * n ** dims / m ** dims, f"ncu capture at {m}^{dims} scaled by cells"
     return None, None
 
 
@@ -996,15 +1001,17 @@ def adjoint_section(n: int, steps: int, every: int, torch_n: int, cpu_n: int = 6
            "state_pool_bytes": steps * 4 * cells if every == 1 else 0,
            "backward_note": f"backward = {recomputed} recomputed forward steps + {steps} adjoint steps "
                             "(24 B/update: read lam, u, k and the gradient of k, write lam and the gradient)"}
+    tf, tf_src = profile_traffic("diffuse3d_zstage_fp32", n, dims=3)
     out["roofline"] = {"bound": "hbm", "achieved": out["forward_gbs"], "peak": hbm, "unit": "GB/s",
-                       "frac": out["forward_gbs"] / hbm, "peak_source": src,
+                       "frac": out["forward_gbs"] / hbm, "peak_source": src, "traffic": tf, "traffic_source": tf_src,
                        "kernel_ms": f / steps * 1e3, "algorithmic_bytes_per_launch": 12.0 * cells,
                        "note": "forward staged z-walk kernel, one launch per step (read u, k; write u)"}
     if every == 1:
         ab = 24.0 * cells * steps / bwd / 1e9
+        ta, ta_src = profile_traffic("diffuse3d_zstage_fp32", n, key="adjoint_traffic_bytes_per_launch_", dims=3)
         out["adjoint_roofline"] = {"bound": "hbm", "achieved": ab, "peak": hbm, "unit": "GB/s", "frac": ab / hbm,
-                                   "peak_source": src, "kernel_ms": bwd / steps * 1e3,
-                                   "algorithmic_bytes_per_launch": 24.0 * cells,
+                                   "peak_source": src, "kernel_ms": bwd / steps * 1e3, "traffic": ta,
+                                   "traffic_source": ta_src, "algorithmic_bytes_per_launch": 24.0 * cells,
                                    "note": "adjoint step kernel; backward time / steps (the backward pass is the "
                                            "adjoint launches only)"}
         cf, cb, _ = run_ours(n, steps, interval=20)
