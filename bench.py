@@ -459,6 +459,7 @@ def launch_times(native_k, step, flush=None):
 JACOBI_FP64_OPS = 4
 JACOBI_ITERS = 50     # pressure iterations of the loop in the cavity step
 LOOP_SITE = 61        # profiling site (group * 64 + 61) of a persistent loop launch
+TLOOP_SITE = 57       # profiling site (group * 64 + 57) of a launch of several loop iterations
 
 
 def gpu_bench(args, rank: int, world: int):
@@ -534,14 +535,17 @@ def gpu_bench(args, rank: int, world: int):
     dom_avg_s = secs / args.steps * share / dom_per_step
     node_avg_s = statistics.mean(dom_ms) / 1000.0
     group = dom_site // 64
-    # a persistent loop launch runs all 50 Jacobi iterations (+ boundary phases)
+    # a persistent loop launch runs all 50 Jacobi iterations (+ boundary phases), a
+    # temporal loop launch up to loop_temporal of them (50 / its launches per step)
     loop = dom_site % 64 == LOOP_SITE
-    iters = JACOBI_ITERS if loop else 1
+    tl = dom_site % 64 == TLOOP_SITE
+    iters = JACOBI_ITERS if loop else (JACOBI_ITERS / dom_per_step if tl else 1)
     bytes_per_cell = algorithmic_bytes(native_k.module, group)
     alg_bytes = bytes_per_cell * n * n * iters
     hbm_peak, peak_src = peaks()
     achieved = alg_bytes / dom_avg_s / 1e9
-    traffic, traffic_src = profile_traffic("cavity_jacobi_loop_fp64" if loop else "cavity_jacobi_fused_fp64", n)
+    traffic, traffic_src = profile_traffic("cavity_jacobi_loop_fp64" if loop else
+                                           ("cavity_jacobi_tloop_fp64" if tl else "cavity_jacobi_fused_fp64"), n)
     pow2 = ((n - 1) & (n - 2)) == 0
     fp64 = None
     if pow2:
@@ -591,7 +595,8 @@ def gpu_bench(args, rank: int, world: int):
                      "frac": achieved / hbm_peak, "traffic": traffic, "traffic_source": traffic_src,
                      "peak_source": peak_src,
                      "kernel": f"group {group} (site {dom_site}"
-                               f"{', persistent loop: %d iterations per launch' % iters if loop else ''})",
+                               f"{', persistent loop: %d iterations per launch' % iters if loop else ''}"
+                               f"{', %g iterations per launch on shared-memory boxes' % iters if tl else ''})",
                      "kernel_ms": dom_avg_s * 1e3,
                      "kernel_time": "ms_per_step x kernel_share / launches of the kernel per step",
                      "kernel_share": share, "share_source": time_src, "kernel_launches_per_step": dom_per_step,
@@ -803,12 +808,16 @@ def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
     for mode, tag, bpc, site in ((None, "fp64_jacobi", 24.0, 127), ("fp32", "fp32_defect", 12.0, 123)):
         k, args, _ = kernels[mode]
         by_site, nsteps, time_src = launch_times(k.native, lambda: k(*args))
+        if mode is None and 64 + TLOOP_SITE in by_site:
+            site = 64 + TLOOP_SITE  # several Jacobi iterations per launch
         if site not in by_site:
             continue
         ms = by_site[site]
         total = sum(sum(v) for v in by_site.values())
         share = sum(ms) / total
         per_step = len(ms) / nsteps
+        if site == 64 + TLOOP_SITE:
+            bpc = bpc * JACOBI_ITERS / per_step
         ks = out["fp64" if mode is None else mode]["ms_per_step"] * 1e-3 * share / per_step
         rl[tag] = {"bound": "hbm", "achieved": bpc * n * n / ks / 1e9, "peak": hbm_peak, "unit": "GB/s",
                    "frac": bpc * n * n / ks / 1e9 / hbm_peak, "peak_source": src, "kernel_ms": ks * 1e3,

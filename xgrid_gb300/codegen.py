@@ -396,7 +396,7 @@ class CudaGenerator:
         fusable launch group and every load of the rewritten grid reads level 0:
         each iteration is then the same launch with the level and the scratch
         buffer exchanged."""
-        if not (self.cfg.persistent and self.cfg.fuse) or not loop.body:
+        if not ((self.cfg.persistent or self.cfg.loop_temporal >= 2) and self.cfg.fuse) or not loop.body:
             return None
         key = ("loop", id(loop))
         if key in self._plans:
@@ -454,16 +454,24 @@ class CudaGenerator:
         out.append(f"{indent}  for ({v} = {self.expr(loop.start, env)}; {v} < {self.expr(loop.end, env)}; "
                    f"{v} += {self.expr(loop.step, env)}) ++xg_K;")
         out.append(f"{indent}  if (xg_K > 0) {{")
-        out.append(f"{indent}    const int xg_r = xg_fuse_{n} ? xgl_{n}_{gid}_loop(xg_G, &xg_h, xg_K, xg_s) : 0;")
+        # a persistent loop when asked for, else several iterations per launch, else one
+        if self.cfg.persistent:
+            out.append(f"{indent}    int xg_r = xg_fuse_{n} ? xgl_{n}_{gid}_loop(xg_G, &xg_h, xg_K, xg_s) : 0;")
+            out.append(f"{indent}    if (xg_r == 0 && xg_fuse_{n}) xg_r = xgl_{n}_{gid}_tloop(xg_G, &xg_h, xg_K, xg_s);")
+        else:
+            out.append(f"{indent}    int xg_r = xg_fuse_{n} ? xgl_{n}_{gid}_tloop(xg_G, &xg_h, xg_K, xg_s) : 0;")
         out.append(f"{indent}    if (xg_r < 0) return xg_r;")
         out.append(f"{indent}    if (xg_r == 0) for (int64_t xg_i = 0; xg_i < xg_K; ++xg_i) "
                    f"XG_TRY(xgl_{n}_{gid}(xg_G, &xg_h, xg_s));")
         out.append(f"{indent}  }}")
         out.append(f"{indent}}}")
         em.emit_kernels()
-        em.emit_loop()
+        from . import tloop
+        tloop.emit(em, self.cfg.loop_temporal)
         self.group_emitters.append(em)
-        self.loop_groups.append(gid)
+        if self.cfg.persistent:
+            em.emit_loop()
+            self.loop_groups.append(gid)
 
     # ================================================================ sweeps
     def emit_run(self, run: list, env, indent: str, out: list) -> None:
@@ -543,6 +551,7 @@ class CudaGenerator:
         src.append(f"static int xg_fuse_{name} = {1 if self.cfg.fuse else 0};")
         src.append(f"static int xg_zstage_{name} = 1;  // staged z-walk of mask-free 3-D sweeps (0: register z-walk)")
         src.append(f"static long long xg_zstage_launches_{name} = 0;  // staged z-walk launches issued by the host")
+        src.append(f"static int xg_tloop_{name} = 1;  // several loop iterations per launch where possible (0: one)")
         # launch hook (slab decomposition): called before every single-sweep launch with the
         # launch's site (group * 64 + sweep), so that a caller can refresh halo rows first
         src.append(f"static xg_launch_hook_fn xg_hook_{name} = NULL;")
@@ -573,6 +582,7 @@ class CudaGenerator:
         src.append(f'extern "C" int xg_groups_{name}(void) {{ return {self.group_counter[0]}; }}')
         src.append(f'extern "C" int xg_zstage_set_{name}(int on) {{ xg_zstage_{name} = on; return 0; }}')
         src.append(f'extern "C" long long xg_zstage_launches_get_{name}(void) {{ return xg_zstage_launches_{name}; }}')
+        src.append(f'extern "C" int xg_tloop_set_{name}(int on) {{ xg_tloop_{name} = on; return 0; }}')
         src.append(f'extern "C" int xg_set_hook_{name}(xg_launch_hook_fn fn, void* ctx) {{')
         src.append(f"  xg_hook_{name} = fn;")
         src.append(f"  xg_hook_ctx_{name} = ctx;")

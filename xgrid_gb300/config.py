@@ -38,6 +38,13 @@ Backend options (new keywords, all optional):
   tiles' previous iteration (per-tile completion flags), instead of one launch
   per iteration; same arithmetic, same bits.  Calls of one module with this
   option must not overlap on the GPU (the flags are a module-wide array).
+* ``loop_temporal``: iterations per launch of an in-place loop of that kind on
+  2-D grids under overstep "none" whose level fits in a quarter of L2 (boxes of
+  the grid staged in shared memory with a halo of that many cells, recomputed per
+  iteration; ``xgrid_gb300.tloop``; default 3, the fastest of 2/3/4 measured on a
+  GB300 for the 1025^2 cavity); 0 or 1: one launch per iteration.  Same arithmetic per cell, same bits; applies
+  only when the box check proves every read exact, else one launch per
+  iteration.
 * ``fail_waits``: for testing only.  Compile modules whose give-up waits cannot
   succeed (the neighbour-tile wait of a persistent loop polls once; a TMA
   staging barrier expects more bytes than its copies deliver), so that those waits run
@@ -88,6 +95,7 @@ class Configuration:
     int_adds: int = 0
     persistent: bool = False
     fail_waits: bool = False
+    loop_temporal: int = 3
 
     def __repr__(self) -> str:
         return repr(dataclasses.asdict(self))
@@ -121,7 +129,7 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
          exact: bool = True, mixed: Optional[str] = None, graph: bool = True,
          fuse: bool = True, divisor: bool = True, mixed_every: int = 0, autotune: bool = True,
          mixed_temporal: int = 8, mixed_rows: int = 8, int_adds: int = 0, persistent: bool = False,
-         fail_waits: bool = False) -> None:
+         fail_waits: bool = False, loop_temporal: int = 3) -> None:
     """Set the global configuration (same keywords as the reference plus GPU options)."""
     global _config
     if sys.version_info < (3, 10):
@@ -138,10 +146,12 @@ def init(*, parallel: bool = True, cc: list = ["gcc", "clang"], cacheroot: str =
         logger.dead(f"Invalid mixed_temporal {mixed_temporal}: 0 (off) to 16 iterations per launch")
     if int(int_adds) < 0:
         logger.dead(f"Invalid int_adds {int_adds}: 0 (off) or every n-th addition")
+    if not 0 <= int(loop_temporal) <= 8:
+        logger.dead(f"Invalid loop_temporal {loop_temporal}: 0 (off) to 8 iterations per launch")
     if int(mixed_rows) not in MIXED_ROWS:
         logger.dead(f"Invalid mixed_rows {mixed_rows}, expected one of {MIXED_ROWS}")
     _config = Configuration(parallel, list(cc), cacheroot, comment, overstep, opt_level,
                             precision, exact, mixed, graph, fuse, divisor, int(mixed_every), bool(autotune),
                             int(mixed_temporal), int(mixed_rows), int(int_adds), bool(persistent),
-                            bool(fail_waits))
+                            bool(fail_waits), int(loop_temporal))
     logger.info(f"initialized with configuration: {_config}")

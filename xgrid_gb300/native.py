@@ -69,6 +69,15 @@ class NativeKernel:
         fn(ctypes.c_int(1 if on else 0))
         runtime.load().xg_graph_clear(self.fn_ptr)
 
+    def set_tloop(self, on: bool) -> None:
+        """Several iterations of an in-place loop per launch where the box check
+        allows it (the default, ``loop_temporal`` iterations), or one launch per
+        iteration."""
+        fn = getattr(self.lib.dylib, f"xg_tloop_set_{self.module.name}")
+        fn.restype = ctypes.c_int
+        fn(ctypes.c_int(1 if on else 0))
+        runtime.load().xg_graph_clear(self.fn_ptr)
+
     def zstage_launches(self) -> int:
         """Staged z-walk launches this module's host code has issued (graph
         replays re-run captured launches without counting)."""
