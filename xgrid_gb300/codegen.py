@@ -54,7 +54,6 @@ ZSTAGE_THREADS = 256
 ZSTAGE_AHEAD = 1
 ZSTAGE_AHEAD_WIDE = 1  # with three or more staged buffers (three CTAs per SM still fit)
 ZSTAGE_MAX_BLOCKS = 3
-ZSTAGE_SHUFFLE = False
 ZSTAGE_ONE_BARRIER = True
 
 # (tz, ty, tx, block.x, block.y, block.z) per grid dimensionality
@@ -961,9 +960,7 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
     is null.  The parameter struct has Z, Y, X."""
     g = zstage_geometry(T, len(srcs))
     V, NTX, NTY, RY, D, PX, TY, TX, R = (g[k] for k in ("V", "NTX", "NTY", "RY", "D", "PX", "TY", "TX", "R"))
-    # x-neighbours from the adjacent lanes when a warp covers whole rows (measured slower than
-    # reading them from the ring: the shuffle waits for the vector load)
-    shuffle = ZSTAGE_SHUFFLE and NTX % 32 == 0
+
     VT = "double2" if T == "double" else "float4"
     nb = len(srcs)
     comp = "xyzw"
@@ -1072,16 +1069,9 @@ def zstage_frame(kname: str, ptype: str, T: str, srcs: list, loads: list, outs: 
             K.append(f"        const {VT} {w} = zw{b}_{'m' if oz < 0 else 'c'}[i];")
         else:
             K.append(f"        const {VT} {w} = *reinterpret_cast<const {VT}*>(&{base}]);")
-        last = comp[V - 1]
-        if -1 in oxs and shuffle:
-            K.append(f"        const {T} {w}_ls = __shfl_up_sync(0xffffffffu, {w}.{last}, 1);")
-            K.append(f"        const {T} {w}_l = (tx_t & 31) == 0 ? {base} - 1] : {w}_ls;")
-        elif -1 in oxs:
+        if -1 in oxs:
             K.append(f"        const {T} {w}_l = {base} - 1];")
-        if 1 in oxs and shuffle:
-            K.append(f"        const {T} {w}_rs = __shfl_down_sync(0xffffffffu, {w}.x, 1);")
-            K.append(f"        const {T} {w}_r = (tx_t & 31) == 31 ? {base} + V] : {w}_rs;")
-        elif 1 in oxs:
+        if 1 in oxs:
             K.append(f"        const {T} {w}_r = {base} + V];")
     for o, _ in enumerate(outs):
         K.append(f"        {T} o{o}[V];")

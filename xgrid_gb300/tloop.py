@@ -37,7 +37,8 @@ from __future__ import annotations
 from . import analysis
 
 THREADS = 256
-SITE = 57  # profiling site of the launch within its group
+SITE = 57
+MIN_BLOCKS = 2  # resident CTAs per SM asked of ptxas  # profiling site of the launch within its group
 
 
 def plan(em) -> dict | None:
@@ -125,7 +126,7 @@ def emit(em, th: int) -> None:
         env = SweepEnv(gen, em.hoist_map, names, em.div_map, em.mul_map)
         return lines, gen.expr(sweep.stmt.value, env)
 
-    K = [f"template <typename I, int BX> __global__ void __launch_bounds__({THREADS}, 2) "
+    K = [f"template <typename I, int BX> __global__ void __launch_bounds__({THREADS}, {MIN_BLOCKS}) "
          f"xgk_{n}_{gid}_tl(const __grid_constant__ struct xgp_{n}_{gid}_tl p) {{",
          f"  constexpr int TH = {th}, NT = {THREADS};",
          "  extern __shared__ __align__(16) unsigned char xg_tl_raw[];",
@@ -152,14 +153,15 @@ def emit(em, th: int) -> None:
          f"  {T}* Sb = S1;",
          "  for (int k = 1; k <= p.iters; ++k) {",
          "    // cells at distance >= k from the box edge are exact after iteration k",
-         "    for (int l = tid; l < NB; l += NT) {",
-         "      const int ly = l / BX, lx = l % BX;",
-         "      const int gy = gy0 + ly, gx = gx0 + lx;",
-         "      if (ly < k || ly >= BY - k || lx < k || lx >= BX - k || gy < 0 || gy >= Y || gx < 0 || gx >= X) "
-         "continue;",
-         "      const I g = (I)gy * X + gx;",
-         "      (void)g;",
-         "      if (zero || MK[l] == 0) {"]
+         ]
+    K += ["    for (int l = tid; l < NB; l += NT) {",
+          "      const int ly = l / BX, lx = l % BX;",
+          "      const int gy = gy0 + ly, gx = gx0 + lx;",
+          "      if (ly < k || ly >= BY - k || lx < k || lx >= BX - k || gy < 0 || gy >= Y || gx < 0 || gx >= X) "
+          "continue;",
+          "      const I g = (I)gy * X + gx;",
+          "      (void)g;",
+          "      if (zero || MK[l] == 0) {"]
     pre, val = cell_code(sweeps[0], "Sa", "        ")
     K += pre + [f"        Sb[l] = {val};",
                 "      } else {",
