@@ -636,6 +636,10 @@ def diffusion_section(n: int = 512, steps: int = 500, runs: int = 3, cpu_seconds
     for _ in range(steps):
         k(u, c)
     digests = [hashlib.sha256(u.read(lv).tobytes()).hexdigest() for lv in range(2)]
+    # the tile shape picked by timing candidates on this grid (state restored afterwards), as for
+    # the headline
+    from xgrid_gb300 import autotune
+    tilings = {str(g): list(t) for g, t in autotune.tune(k, u, c).items()}
     parity = None
     try:
         ref = json.load(open(os.path.join(ROOT, "tests", "golden", "full_digests.json")))["diffusion_512"]
@@ -702,7 +706,7 @@ def diffusion_section(n: int = 512, steps: int = 500, runs: int = 3, cpu_seconds
         "config": f"2-D FTCS diffusion {n}x{n} FP64, u0 ~ U[0,1) seed 0, c = 0.2, zero edges, {steps} steps "
                   f"(one kernel call per step, graph replay per call)",
         "value": lups / run_s / 1e9, "unit": "GLUP/s", "ms_per_run": run_s * 1e3, "steps_per_run": steps,
-        "parity": parity,
+        "parity": parity, "tilings": tilings,
         "whole_run_graph": {"value": lups / graph_run_s / 1e9, "unit": "GLUP/s", "ms_per_run": graph_run_s * 1e3,
                             "what": f"the {steps} calls captured into one CUDA graph and replayed (no per-call "
                                     f"host work)"},
@@ -740,7 +744,7 @@ def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
     from xgrid_gb300.operator import Operator
 
     dt = stable_dt(n)
-    out, fields, kernels = {}, {}, {}
+    out, fields, kernels, tuned = {}, {}, {}, {}
     for mode in (None, "fp32", "fp16", "bf16"):
         xgrid.init(precision="double", cacheroot=JIT_CACHE,
                    opt_level=3, mixed=mode, mixed_temporal=temporal)
@@ -748,6 +752,9 @@ def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
         grids, cfg = workloads.cavity_setup(n, dt)
         args = (grids["b"], grids["p"], grids["u"], grids["v"], cfg)
         kernels[mode] = (k, args, grids)
+        # tile shapes of the launch groups timed on these grids (state restored afterwards)
+        from xgrid_gb300 import autotune
+        tuned[mode or "fp64"] = {str(g): list(t) for g, t in autotune.tune(k, *args).items()}
         half = steps // 2
         for _ in range(steps - half):
             k(*args)
@@ -762,7 +769,7 @@ def mixed_section(n: int, steps: int, temporal: int = 4) -> dict:
         fields[mode] = {g: grids[g].read(0) for g in "puv"}
         out["fp64" if mode is None else mode] = {"ms_per_step": ms, "steps_per_s": 1e3 / ms,
                                                  "value": SWEEPS_PER_STEP * n * n / (ms * 1e-3) / 1e9,
-                                                 "unit": "GLUP/s"}
+                                                 "unit": "GLUP/s", "tilings": tuned[mode or "fp64"]}
     # algorithmic bytes per cell and step.  "sweep" counts every pressure iteration as one
     # sweep without temporal reuse (50 FP64 Jacobi sweeps, or residual + 49 defect iterations +
     # correction); "launch" counts what the launches of the mixed path must move at least: the
