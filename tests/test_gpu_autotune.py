@@ -103,3 +103,28 @@ def test_even_tile_rows_keep_the_bits(cacheroot, tiling, persistent):
         tiled(*a)
         plain(*b)
     assert _state(ga) == _state(gb)
+
+
+def test_tuning_fresh_grids_keeps_their_state(cacheroot, monkeypatch):
+    """Tuning before the first call (levels not yet on the device, zero or written
+    on the host) leaves the grids as a first call finds them: the run that follows
+    gives the bits of an untuned run."""
+    import os
+    n = 129
+    xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3)
+    monkeypatch.setattr(autotune, "CACHE_FILE", "autotune_fresh.json")
+    path = os.path.join(cacheroot, "autotune_fresh.json")
+    if os.path.exists(path):
+        os.remove(path)
+    out = []
+    for tune in (True, False):
+        k = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
+        grids, cfg = workloads.cavity_setup(n, 1e-4)
+        grids["u"].now[5:9, 5:9] = 0.25  # a host-written level next to zero ones
+        a = (grids["b"], grids["p"], grids["u"], grids["v"], cfg)
+        if tune:
+            autotune.tune(k, *a)
+        for _ in range(3):
+            k(*a)
+        out.append(_state(grids))
+    assert out[0] == out[1]

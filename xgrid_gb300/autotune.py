@@ -89,7 +89,14 @@ class Snapshot:
                 for lv, copy, auth in copies:
                     if copy is not None:
                         lv.dev.copy_(copy)
-                    lv.auth = auth
+                        lv.auth = auth
+                    elif lv.dev is not None and auth == "zero":
+                        # a level that had no device buffer and was zero: the timed calls
+                        # allocated and wrote one; zero it and let it stand for the level
+                        lv.dev.zero_()
+                        lv.auth = "dev"
+                    else:
+                        lv.auth = auth  # "host": the host copy is uploaded at the next call
         device.stream().synchronize()
 
 
