@@ -36,15 +36,16 @@ def _state(grids):
     return {g: (grids[g].read(0).tobytes(), grids[g].read(1).tobytes()) for g in "bpuv"}
 
 
-@pytest.mark.parametrize("n,th", [(257, 2), (257, 3), (257, 4), (1025, 2), (130, 3)])
-def test_boxes_give_the_bits_of_one_launch_per_iteration(cacheroot, n, th):
+@pytest.mark.parametrize("n,th,precision", [(257, 2, "double"), (257, 3, "double"), (257, 4, "double"),
+                                             (1025, 2, "double"), (130, 3, "double"), (201, 3, "float")])
+def test_boxes_give_the_bits_of_one_launch_per_iteration(cacheroot, n, th, precision):
     # the reference path: a module generated with one launch per iteration
-    xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3, loop_temporal=0)
+    xgrid.init(precision=precision, cacheroot=cacheroot, opt_level=3, loop_temporal=0)
     single = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
     gb, cfg = workloads.cavity_setup(n, 5e-6, seed=11)
     b = (gb["b"], gb["p"], gb["u"], gb["v"], cfg)
     single(*b)
-    xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3, loop_temporal=th)
+    xgrid.init(precision=precision, cacheroot=cacheroot, opt_level=3, loop_temporal=th)
     boxed = Operator(workloads.cavity_kernel.func, "kernel", "cavity_kernel")
     ga, _ = workloads.cavity_setup(n, 5e-6, seed=11)
     a = (ga["b"], ga["p"], ga["u"], ga["v"], cfg)
