@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product path imports this package;
 tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use it
-as the checker.
+to check results.
 
 It interprets the typed IR (shared front end) the way the reference's generated
 C executes (xgrid/lang/generator.py):
