@@ -193,3 +193,50 @@ def test_noalloc_entry_is_exported_by_every_kind_of_kernel(tmp_path):
         lib = Compiler(cacheroot=str(tmp_path)).compile(m.source, get_config().nvcc_flags)
         out = __import__("subprocess").run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True).stdout
         assert f"xg_kernel_{fn.__name__}_noalloc" in out
+
+
+def wrap_relax(p: xgrid.grid[float, 2], f: xgrid.grid[float, 2], iters: int) -> None:
+    for _ in range(0, iters):
+        p[0, 0] = 0.25 * (p[1, 0][0] + p[-1, 0][0] + p[0, 1][0] + p[0, -1][0]) - f[0, 0][0]
+
+
+def wide_relax(p: xgrid.grid[float, 2], f: xgrid.grid[float, 2], iters: int) -> None:
+    for _ in range(0, iters):
+        p[0, 0] = 0.25 * (p[2, 0][0] + p[-1, 0][0] + p[0, 1][0] + p[0, -1][0]) - f[0, 0][0]
+
+
+def test_loop_iterations_per_launch_plan():
+    """Several pressure iterations per launch: generated for the cavity's loop (main
+    sweep reaching one cell, four boundary phases) and for a loop of one sweep when
+    ``loop_temporal`` >= 2; not for reads reaching two cells, for periodic grids
+    (overstep "wrap"), or with ``loop_temporal`` 0 -- there the launcher is a stub
+    that declines."""
+    def source(fn, name, **cfg):
+        xgrid.init(precision="double", cacheroot="/tmp/xgcg", opt_level=3, **cfg)
+        return CudaGenerator(Operator(fn, "kernel", name), get_config()).generate().source
+
+    src = source(workloads.cavity_kernel.func, "cavity_kernel")
+    assert "xgk_cavity_kernel_1_tl<" in src and "xgl_cavity_kernel_1_tloop(xg_G" in src
+    assert "static const int32_t vals[] = {1, 2, 3, 4};" in src
+    assert "constexpr int TH = 3" in src
+    src = source(workloads.cavity_kernel.func, "cavity_kernel", loop_temporal=0)
+    assert "_tl<" not in src and "return 0; }" in src
+    for fn, cfg in ((wide_relax, {}), (wrap_relax, {"overstep": "wrap"})):
+        src = source(fn, fn.__name__, **cfg)
+        assert "_tl<" not in src, fn.__name__
+    assert "_tl<" in source(wrap_relax, "wrap_relax")
+
+
+def test_staged_geometry_fits_the_sm():
+    """Staged z-walk shapes: whole 16-byte vectors per thread, whole rows per
+    thread, shared memory that leaves at least one CTA per SM (three for FP32)."""
+    from xgrid_gb300 import codegen
+    for T in ("float", "double"):
+        for nb in (1, 2, 3, 4):
+            g = codegen.zstage_geometry(T, nb)
+            assert g["NTX"] * g["V"] == g["TX"] and g["NTX"] * g["NTY"] == codegen.ZSTAGE_THREADS
+            assert g["RY"] * g["NTY"] == g["TY"] and g["PX"] % g["V"] == 0
+            assert g["R"] in (g["D"] + 3, g["D"] + 4) and g["blocks"] >= 1
+            assert g["blocks"] * (g["smem"] + 1024) <= 228 * 1024
+            if T == "float" and nb <= 3:
+                assert g["blocks"] == 3

@@ -93,3 +93,37 @@ def test_reads_beyond_the_grid_fall_back(cacheroot):
         out.append(p.read(0))
     assert not any(s % 64 == TLOOP_SITE for s in sites[0])
     assert out[0].tobytes() == out[1].tobytes()
+
+
+def plain_relax(p: xgrid.grid[float, 2], f: xgrid.grid[float, 2], iters: int) -> None:
+    for _ in range(0, iters):
+        p[0, 0] = 0.25 * (p[1, 0][0] + p[-1, 0][0] + p[0, 1][0] + p[0, -1][0]) - f[0, 0][0]
+
+
+@pytest.mark.parametrize("iters", [7, 2, 1])
+def test_loop_of_one_sweep_on_boxes(cacheroot, iters):
+    """A loop of one Jacobi sweep (a frame of boundary cells that no sweep writes)
+    runs on boxes too, with the bits of one launch per iteration, for iteration
+    counts that leave remainders and for a single iteration (one plain launch)."""
+    shape = (150, 211)
+    rng = np.random.default_rng(8)
+    p0, f0 = rng.random(shape), rng.random(shape)
+    m = np.zeros(shape, np.int32)
+    m[0, :] = m[-1, :] = m[:, 0] = m[:, -1] = 1
+    out, sites = [], []
+    for th in (3, 0):
+        xgrid.init(precision="double", cacheroot=cacheroot, opt_level=3, loop_temporal=th)
+        k = Operator(plain_relax, "kernel", "plain_relax")
+        p, f = xgrid.Grid(shape, float), xgrid.Grid(shape, float)
+        p._extend_time(2)
+        for lv in p._data:
+            lv[...] = p0
+        f.now[...] = f0
+        p.boundary[...] = m
+        k(p, f, iters)
+        sites.append(_sites(k, lambda: k(p, f, iters)))
+        out.append(p.read(0))  # the kernel reads time level 0 only: one level
+    boxed = sum(1 for s in sites[0] if s % 64 == TLOOP_SITE)
+    assert boxed == (-(-iters // 3) if iters > 1 else 0)
+    assert not any(s % 64 == TLOOP_SITE for s in sites[1])
+    assert out[0].tobytes() == out[1].tobytes()

@@ -423,7 +423,10 @@ class CudaGenerator:
                 return None
         counter = [self.group_counter[0]]
         groups = analysis.build_groups(sweeps, counter, True)
-        if len(groups) != 1 or not groups[0].fusable or groups[0].sweeps[0] is not sweeps[0]:
+        # a persistent loop runs the fused kernel; several iterations per launch also take a
+        # loop of one sweep
+        single = len(groups) == 1 and len(groups[0].sweeps) == 1 and not self.cfg.persistent
+        if len(groups) != 1 or not (groups[0].fusable or single) or groups[0].sweeps[0] is not sweeps[0]:
             return None
         if any(sw.write_version != 1 for sw in sweeps) or sweeps[0].read_version_of_target != 0:
             return None
