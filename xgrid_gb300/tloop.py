@@ -1,8 +1,8 @@
 """Several iterations of an in-place loop per launch, bit-exact (2-D grids).
 
-A loop whose body is one implicit main sweep of a grid ``p`` followed by
-boundary phases of ``p`` (the cavity's pressure iterations,
-examples/cavity.py:99-113) normally costs one launch per iteration, and at
+A loop whose body is one implicit main sweep of a grid ``p``, alone or followed
+by boundary phases of ``p`` (the cavity's pressure iterations,
+examples/cavity.py:99-113), normally costs one launch per iteration, and at
 sizes whose working set sits in L2 the fixed cost of a launch (its ramp and
 tail, ~4-5 us on GB300) is a third of an FP64 Jacobi sweep.  Here a launch runs
 up to ``TH`` iterations of the group on *boxes*:
