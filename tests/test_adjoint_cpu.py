@@ -43,3 +43,22 @@ def test_shift_moves_every_load():
     node = A.s_mul(("l", (0, 1, (0, 0, 1))), ("l", (1, 0, (0, -1, 0))))
     s = A.shift(node, (0, 0, 1))
     assert A.loads_of(s) == [(0, 1, (0, 0, 0)), (1, 0, (0, -1, -1))]
+
+
+def test_rollout_keeps_every_state_within_the_budget():
+    """The rollout's choice between a state pool and checkpoints (host logic, no
+    GPU): an explicit interval wins; otherwise every state is kept when ``steps``
+    states fit in the budget, else a checkpoint every 20 steps."""
+    import xgrid
+    import workloads
+    from xgrid_gb300.operator import Operator
+    xgrid.init(precision="float", cacheroot="/tmp/xgadj", opt_level=3, overstep="wrap")
+    k = Operator(workloads.diffuse3d.func, "kernel", "diffuse3d")
+    state = 64 ** 3 * 4
+    assert A.Rollout(k, 200, 7).checkpoint_interval(state) == 7
+    assert A.Rollout(k, 200, 1).checkpoint_interval(state) == 1
+    assert A.Rollout(k, 200, state_budget=200 * state).checkpoint_interval(state) == 1
+    assert A.Rollout(k, 200, state_budget=200 * state - 1).checkpoint_interval(state) == 20
+    import pytest
+    with pytest.raises(Exception):
+        A.Rollout(k, 0)
